@@ -1,0 +1,1053 @@
+// api.cu -- the C ABI (include/nudim.h): context, jobs and operator-level
+// entry points, plus the job pipeline that replaces
+// src/reconstruction.c:304-719 with every Z-plane resident on one GPU.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace nudim {
+const char *last_error();
+
+// ================================================================ setup kernels
+// reconstruction.c:345-355: f_hat[x*nz + z] = proj[z][x] (real, imaginary 0)
+__global__ void k_proj_fhat(const double *__restrict__ proj, double2 *__restrict__ fh, int nx,
+                            int nz)
+{
+    int t = blockIdx.y;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx * nz) return;
+    int col = i % nx, row = i / nx;
+    fh[(size_t)t * nx * nz + (size_t)col * nz + row] =
+        make_double2(proj[(size_t)t * nx * nz + i], 0.0);
+}
+
+// reconstruction.c:437-484 in the q order of the Z-frequency volume:
+// plane q holds slice j = (q + nz/2) % nz.
+template <typename T>
+__global__ void k_build_slices(const double2 *__restrict__ tomo, const int *__restrict__ known,
+                               const int *__restrict__ order, const int *__restrict__ unk_rank,
+                               const double *__restrict__ fill, int n_unk_row, int np, int nz,
+                               int M, cplx_t<T> *__restrict__ slices)
+{
+    int q = blockIdx.y;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int j = (q + nz / 2) % nz;
+    int a = i / np, r = i - a * np;
+    double re = 0, im = 0;
+    if (known[a]) {
+        double2 v = tomo[(size_t)order[a] * np * nz + (size_t)j * np + r];
+        re = v.x;
+        im = v.y;
+    } else if (fill) {
+        re = fill[(size_t)j * n_unk_row + unk_rank[i]];
+    }
+    slices[(size_t)q * M + i] = mkc<T>((T)re, (T)im);
+}
+
+__global__ void k_real_cplx(const double *__restrict__ d, double2 *__restrict__ c, size_t n)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) c[i] = make_double2(d[i], 0.0);
+}
+
+// projection_sim.c:344-366: slice_t[row][col] = NFFT of plane j = (row+nz/2)%nz
+// at radius (col+np/2)%np; plane j's NFFT is row `row` of tmp (q order).
+__global__ void k_sim_gather(const double2 *__restrict__ tmp, double2 *__restrict__ sl, int nz,
+                             int np, int M)
+{
+    int t = blockIdx.y;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nz * np) return;
+    int row = i / np, col = i - row * np;
+    sl[(size_t)t * nz * np + i] = tmp[(size_t)row * M + (size_t)t * np + (col + np / 2) % np];
+}
+
+// projection_sim.c:377-390: radial fftshift, real part
+__global__ void k_sim_shift(const double2 *__restrict__ sl, double *__restrict__ out, int nz,
+                            int np)
+{
+    int t = blockIdx.y;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nz * np) return;
+    int row = i / np, col = i - row * np;
+    out[(size_t)t * nz * np + i] = sl[(size_t)t * nz * np + (size_t)row * np + (col + np / 2) % np].x;
+}
+
+// ================================================================ per-precision state
+template <typename T> struct JobState {
+    using C = cplx_t<T>;
+    bool live = false;
+    NfftDev<T> pl;
+    T *img_a = nullptr, *img_b = nullptr, *grad = nullptr, *w = nullptr;
+    C *data = nullptr, *y = nullptr, *r = nullptr, *v = nullptr, *z = nullptr, *p = nullptr,
+      *slices = nullptr;
+    int *known = nullptr;
+    double *part = nullptr, *dots = nullptr, *tv_part = nullptr, *tv_scal = nullptr,
+           *rh = nullptr;
+    int part_stride = 0, tv_cap = 0;
+    size_t bytes = 0;
+    std::vector<void *> owned;
+
+    template <typename P> int alloc(P **ptr, size_t n)
+    {
+        size_t b = sizeof(P) * (n ? n : 1);
+        void *q = nullptr;
+        NUDIM_CUDA(cudaMalloc(&q, b));
+        owned.push_back(q);
+        bytes += b;
+        *ptr = (P *)q;
+        return NUDIM_OK;
+    }
+    void release()
+    {
+        for (void *q : owned) cudaFree(q);
+        owned.clear();
+        pl.release();
+        live = false;
+    }
+};
+
+}  // namespace nudim
+
+using namespace nudim;
+
+struct nudim_job {
+    nudim_ctx *ctx = nullptr;
+    nudim_job_desc d{};
+    int A = 0, M = 0, nmeas = 0, n_unk_row = 0;
+    double pad_min = 0, pad_max = 0;
+    NfftTables tabs;
+    std::vector<int> known, order, unk_rank;
+    std::vector<double> fill;
+    bool fill_set = false, ready = false;
+    int done = 0;
+    JobState<double> s64;
+    JobState<float> s32;
+    int dump_nn = -1;
+    double *dump_before = nullptr, *dump_after = nullptr;
+    std::vector<double> vol0;
+};
+
+struct nudim_nfft_plan {
+    nudim_ctx *ctx = nullptr;
+    int prec = NUDIM_FP64;
+    NfftDev<double> d64;
+    NfftDev<float> d32;
+    // CGNR scratch, grown on demand
+    void *cg = nullptr;
+    size_t cg_bytes = 0;
+};
+
+namespace nudim {
+
+// ================================================================ Z-FFT
+static int zfft_plan(nudim_ctx *ctx, int nz, int P2, int prec, cufftHandle *h)
+{
+    auto key = std::make_tuple(nz, P2, prec, 0);
+    auto it = ctx->fftz.find(key);
+    if (it != ctx->fftz.end()) {
+        *h = it->second;
+        return NUDIM_OK;
+    }
+    cufftHandle p;
+    int n[1] = {nz};
+    // fftw_plan_many_dft(1, &nz, np*np, data, NULL, np*np, 1, ...) (reconstruction.c:556)
+    NUDIM_CUFFT(cufftPlanMany(&p, 1, n, n, P2, 1, n, P2, 1,
+                              prec == NUDIM_FP64 ? CUFFT_Z2Z : CUFFT_C2C, P2));
+    ctx->fftz[key] = p;
+    *h = p;
+    return NUDIM_OK;
+}
+
+template <typename T> static int zfft(nudim_job *jb, JobState<T> &s, int dir)
+{
+    cufftHandle h;
+    int P2 = jb->d.np * jb->d.np;
+    NUDIM_TRY(zfft_plan(jb->ctx, jb->d.nz, P2, prec_of<T>(), &h));
+    NUDIM_CUFFT(cufftSetStream(h, jb->ctx->stream));
+    return fft_exec<T>(h, s.data, dir);
+}
+
+// ================================================================ job state setup
+template <typename T> static int state_init(nudim_job *jb, JobState<T> &s)
+{
+    if (s.live) return NUDIM_OK;
+    int nz = jb->d.nz, np = jb->d.np, M = jb->M;
+    size_t P2 = (size_t)np * np, V = P2 * nz;
+    NUDIM_TRY(s.pl.init(jb->ctx, jb->tabs));
+    s.bytes += s.pl.bytes;
+    NUDIM_TRY(s.alloc(&s.img_a, V));
+    NUDIM_TRY(s.alloc(&s.img_b, V));
+    NUDIM_TRY(s.alloc(&s.data, V));
+    NUDIM_TRY(s.alloc(&s.z, V));
+    NUDIM_TRY(s.alloc(&s.p, V));
+    NUDIM_TRY(s.alloc(&s.y, (size_t)nz * M));
+    NUDIM_TRY(s.alloc(&s.r, (size_t)nz * M));
+    NUDIM_TRY(s.alloc(&s.v, (size_t)nz * M));
+    NUDIM_TRY(s.alloc(&s.slices, (size_t)nz * M));
+    NUDIM_TRY(s.alloc(&s.known, jb->A));
+    NUDIM_CUDA(cudaMemcpyAsync(s.known, jb->known.data(), sizeof(int) * jb->A,
+                               cudaMemcpyHostToDevice, jb->ctx->stream));
+    if (jb->d.weight) {
+        std::vector<double> wd(M);
+        cgnr_weights(jb->A, np, jb->d.padangle, wd.data());
+        std::vector<T> wt(wd.begin(), wd.end());
+        NUDIM_TRY(s.alloc(&s.w, M));
+        NUDIM_CUDA(cudaMemcpyAsync(s.w, wt.data(), sizeof(T) * M, cudaMemcpyHostToDevice,
+                                   jb->ctx->stream));
+        NUDIM_CUDA(cudaStreamSynchronize(jb->ctx->stream));
+    }
+    if (jb->d.denoise == NUDIM_DENOISE_TV) {
+        NUDIM_TRY(s.alloc(&s.grad, V));
+        s.tv_cap = tv_part_count(nz, np, np);
+        NUDIM_TRY(s.alloc(&s.tv_part, s.tv_cap));
+        NUDIM_TRY(s.alloc(&s.tv_scal, 4));
+    }
+    s.part_stride = cgnr_part_stride(M, (int)P2);
+    NUDIM_TRY(s.alloc(&s.part, (size_t)nz * s.part_stride + 2 * (size_t)nz + 2));
+    NUDIM_TRY(s.alloc(&s.dots, (size_t)nz * 4));
+    NUDIM_TRY(s.alloc(&s.rh, (size_t)std::max(1, jb->d.nhio + jb->d.ner)));
+    s.live = true;
+    return NUDIM_OK;
+}
+
+template <typename T> static CgnrBuffers<T> cg_bufs(JobState<T> &s)
+{
+    CgnrBuffers<T> b;
+    b.r = s.r;
+    b.v = s.v;
+    b.z = s.z;
+    b.p = s.p;
+    b.part = s.part;
+    b.part_stride = s.part_stride;
+    b.dots = s.dots;
+    return b;
+}
+
+static int iters_of(const nudim_job *jb) { return jb->d.cgnr_iters > 0 ? jb->d.cgnr_iters : kCgnrIters; }
+
+// Slices, initial inverse NFFT and backward Z-FFT for state s.
+template <typename T>
+static int state_setup(nudim_job *jb, JobState<T> &s, const double2 *tomo, const int *d_order,
+                       const int *d_rank, const double *d_fill)
+{
+    cudaStream_t st = jb->ctx->stream;
+    int nz = jb->d.nz, np = jb->d.np, M = jb->M;
+    size_t P2 = (size_t)np * np;
+    k_build_slices<T><<<dim3(ceil_div(M, 256), nz), 256, 0, st>>>(
+        tomo, s.known, d_order, d_rank, d_fill, jb->n_unk_row, np, nz, M, s.slices);
+    NUDIM_LAUNCH_CHECK();
+    // reconstruction.c:495-518: f = 0, before_loop + 10 steps, per plane
+    CgnrBuffers<T> b = cg_bufs(s);
+    NUDIM_TRY(cgnr_run<T>(s.pl, nz, s.slices, s.w, s.data, nullptr, true, iters_of(jb), b, st));
+    // :521-540 backward Z-FFT, img[(j + nz/2) % nz] = Re(data[j]) / nz
+    NUDIM_TRY(zfft<T>(jb, s, CUFFT_INVERSE));
+    NUDIM_TRY(launch_unpack<T>(s.data, s.img_a, nz, P2, st));
+    return NUDIM_OK;
+}
+
+// One outer HIO/ER iteration nn (reconstruction.c:545-703) on state s.
+template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, int nn)
+{
+    cudaStream_t st = jb->ctx->stream;
+    const nudim_job_desc &d = jb->d;
+    int nz = d.nz, np = d.np, M = jb->M;
+    size_t P2 = (size_t)np * np, V = P2 * nz;
+    // :548-559 data[t] = img[(t+nz/2)%nz]; forward Z-FFT
+    NUDIM_TRY(launch_pack<T>(s.img_a, s.data, nz, P2, st));
+    NUDIM_TRY(zfft<T>(jb, s, CUFFT_FORWARD));
+    // :565-582 per plane: trafo, reciprocal constraint, R-factor partials
+    PadArgs<T> pa;
+    pa.src = s.data;
+    pa.src_stride = P2;
+    InterpArgs<T> ia;
+    ia.mode = IM_CONSTRAINT;
+    ia.out = s.y;
+    ia.out_stride = M;
+    ia.s = s.slices;
+    ia.s_stride = M;
+    ia.known = s.known;
+    ia.line_len = np;
+    ia.part = s.part;
+    ia.part_stride = s.part_stride;
+    NUDIM_TRY(s.pl.trafo(nz, pa, ia, st));
+    NUDIM_TRY(launch_finish_r<T>(s.part, s.pl.interp_blocks(), nz, s.part_stride, s.rh, nn, st));
+    // :587-599 warm start from the real-space plane, CGNR, write back
+    CgnrBuffers<T> b = cg_bufs(s);
+    NUDIM_TRY(cgnr_run<T>(s.pl, nz, s.y, s.w, s.data, s.img_a, false, iters_of(jb), b, st));
+    // :607-621 backward Z-FFT, img = Re(shifted data)/nz
+    NUDIM_TRY(zfft<T>(jb, s, CUFFT_INVERSE));
+    NUDIM_TRY(launch_unpack<T>(s.data, s.img_b, nz, P2, st));
+    // :624-669 denoise
+    bool dump = (nn == jb->dump_nn) && jb->dump_before && d.denoise != NUDIM_DENOISE_NONE;
+    if (dump) {
+        NUDIM_TRY(launch_to_double<T>(s.img_b, (double *)s.z, V, st));
+        NUDIM_CUDA(cudaMemcpyAsync(jb->dump_before, s.z, sizeof(double) * V,
+                                   cudaMemcpyDeviceToHost, st));
+        NUDIM_CUDA(cudaStreamSynchronize(st));
+    }
+    if (d.denoise == NUDIM_DENOISE_DIFFUSION) {
+        float lam = d.variant == NUDIM_VARIANT_PARALLEL ? 0.4f : 0.25f;
+        NUDIM_TRY(diffusion_run<T>(s.img_b, nz, np, np, nz, lam, 0.005f, 80, st));
+    } else if (d.denoise == NUDIM_DENOISE_TV) {
+        bool h = d.height && d.variant == NUDIM_VARIANT_SERIAL;
+        int ylo = (2 * d.ncenter - d.nheight) / 2, yhi = (2 * d.ncenter + d.nheight) / 2;
+        NUDIM_TRY(tv_run<T>(s.img_b, s.grad, s.tv_part, s.tv_cap, s.tv_scal, nz, np, np, 0.2f, 40,
+                            h ? 1 : 0, ylo, yhi, st));
+    }
+    if (dump) {
+        NUDIM_TRY(launch_to_double<T>(s.img_b, (double *)s.z, V, st));
+        NUDIM_CUDA(cudaMemcpyAsync(jb->dump_after, s.z, sizeof(double) * V,
+                                   cudaMemcpyDeviceToHost, st));
+        NUDIM_CUDA(cudaStreamSynchronize(st));
+    }
+    // :672-700 HIO/ER (result lands in img_a: the next img and img_last)
+    int ylo, yhi;
+    if (d.variant == NUDIM_VARIANT_PARALLEL) {
+        ylo = (np - d.nheight) / 2;
+        yhi = (np + d.nheight) / 2;
+    } else {
+        ylo = (2 * d.ncenter - d.nheight) / 2;
+        yhi = (2 * d.ncenter + d.nheight) / 2;
+    }
+    NUDIM_TRY(launch_constraint<T>(s.img_b, s.img_a, nz, np, d.nx, nn < d.nhio ? 1 : 0,
+                                   d.height ? 1 : 0, ylo, yhi, st));
+    return NUDIM_OK;
+}
+
+// FP64 buffers of a mixed job take over from FP32 for one corrective
+// iteration: convert the volume, iterate in FP64, convert back.
+static int corrective_iteration(nudim_job *jb, int nn)
+{
+    cudaStream_t st = jb->ctx->stream;
+    size_t V = (size_t)jb->d.np * jb->d.np * jb->d.nz;
+    NUDIM_TRY(launch_to_double<float>(jb->s32.img_a, jb->s64.img_a, V, st));
+    NUDIM_TRY(state_iterate<double>(jb, jb->s64, nn));
+    NUDIM_TRY(launch_real_to<float>(jb->s64.img_a, jb->s32.img_a, V, st));
+    // keep the FP32 R history complete
+    NUDIM_CUDA(cudaMemcpyAsync(jb->s32.rh + nn, jb->s64.rh + nn, sizeof(double),
+                               cudaMemcpyDeviceToDevice, st));
+    return NUDIM_OK;
+}
+
+static int validate(const nudim_job_desc *d)
+{
+    if (!d) {
+        set_error("null descriptor");
+        return NUDIM_EINVAL;
+    }
+    if (d->nx <= 0 || d->nz <= 0 || d->np <= 0) {
+        set_error("You need to provide valid projection size with --nx, --nz, --pad.");
+        return NUDIM_EINVAL;
+    }
+    if ((d->nz & 1) || (d->np & 1)) {
+        set_error("np and nz must be even (got np=%d nz=%d)", d->np, d->nz);
+        return NUDIM_EINVAL;
+    }
+    if (d->nx > d->np) {
+        set_error("nx (%d) must not exceed np (%d)", d->nx, d->np);
+        return NUDIM_EINVAL;
+    }
+    if (d->nhio < 0 || d->ner < 0) {
+        set_error("You need to provide valid nhio/ner.");
+        return NUDIM_EINVAL;
+    }
+    if (!(d->interval > 0)) {
+        set_error("You need to provide valid angular sampling interval with --interval.");
+        return NUDIM_EINVAL;
+    }
+    if (!(d->padangle > 0) ||
+        d->interval / d->padangle - (int)(d->interval / d->padangle + 0.1) > 1e-5) {
+        set_error("You need to provide valid padded angular sampling interval with --padangle.");
+        return NUDIM_EINVAL;
+    }
+    if (d->gam_max < -90 || d->gam_max > 90 || d->gam_min < -90 || d->gam_min > d->gam_max) {
+        set_error("You need to provide valid scope of tomogram angles (-90,90] with --max, --min.");
+        return NUDIM_EINVAL;
+    }
+    if (d->height && (d->nheight <= 0 || (d->variant == NUDIM_VARIANT_SERIAL && d->ncenter <= 0))) {
+        set_error("You must provide valid both sample height and center with --height and --center.");
+        return NUDIM_EINVAL;
+    }
+    if (d->denoise < 0 || d->denoise > 2 || d->precision < 0 || d->precision > 1 ||
+        d->variant < 0 || d->variant > 1) {
+        set_error("invalid enum value in descriptor");
+        return NUDIM_EINVAL;
+    }
+    return NUDIM_OK;
+}
+
+static size_t job_bytes(const nudim_job_desc *d, int A, bool both)
+{
+    size_t nz = d->nz, np = d->np, P2 = np * np, V = P2 * nz, M = (size_t)A * np;
+    auto per = [&](size_t sT) {
+        size_t sC = 2 * sT;
+        size_t b = 2 * V * sT + 3 * V * sC + 4 * nz * M * sC;
+        if (d->denoise == NUDIM_DENOISE_TV) b += V * sT;
+        b += M * (8 + 28 * sT + 20);  // node tables and tile lists
+        b += nz * (size_t)cgnr_part_stride((int)M, (int)P2) * 8;
+        return b;
+    };
+    size_t b = d->precision == NUDIM_FP64 ? per(8) : per(4);
+    if (both) b += per(8);
+    return b;
+}
+
+}  // namespace nudim
+
+// ================================================================ C ABI
+extern "C" {
+
+const char *nudim_last_error(void) { return nudim::last_error(); }
+int nudim_abi_version(void) { return NUDIM_ABI_VERSION; }
+
+int nudim_ctx_create(int device, unsigned flags, nudim_ctx **out)
+{
+    (void)flags;
+    if (!out) {
+        set_error("null output pointer");
+        return NUDIM_EINVAL;
+    }
+    *out = nullptr;
+    int n = 0;
+    NUDIM_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) {
+        set_error("device %d out of range (%d devices)", device, n);
+        return NUDIM_EINVAL;
+    }
+    NUDIM_CUDA(cudaSetDevice(device));
+    auto *c = new nudim_ctx();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
+    }
+    const char *gb = getenv("NUDIM_GRID_BUDGET_MB");
+    c->grid_budget = gb ? (size_t)atol(gb) << 20 : ((size_t)2 << 30);
+    *out = c;
+    return NUDIM_OK;
+}
+
+int nudim_ctx_destroy(nudim_ctx *c)
+{
+    if (!c) return NUDIM_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto &kv : c->fft2d) cufftDestroy(kv.second);
+    for (auto &kv : c->fftz) cufftDestroy(kv.second);
+    cudaFree(c->ws);
+    cudaFree(c->scratch);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return NUDIM_OK;
+}
+
+void *nudim_ctx_stream(nudim_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int nudim_ctx_sync(nudim_ctx *c)
+{
+    if (!c) return NUDIM_EINVAL;
+    NUDIM_CUDA(cudaStreamSynchronize(c->stream));
+    return NUDIM_OK;
+}
+
+int nudim_job_footprint(const nudim_job_desc *d, size_t *bytes)
+{
+    NUDIM_TRY(validate(d));
+    int A = polar_lines(d->gam_min, d->interval, d->padangle, nullptr, nullptr);
+    *bytes = job_bytes(d, A, d->precision == NUDIM_MIXED && d->correct_every > 0);
+    return NUDIM_OK;
+}
+
+int nudim_job_create(nudim_ctx *ctx, const nudim_job_desc *desc, nudim_job **out)
+{
+    if (!ctx || !out) {
+        set_error("null argument");
+        return NUDIM_EINVAL;
+    }
+    *out = nullptr;
+    NUDIM_TRY(validate(desc));
+    NUDIM_CUDA(cudaSetDevice(ctx->device));
+    std::unique_ptr<nudim_job> jb(new nudim_job());
+    jb->ctx = ctx;
+    jb->d = *desc;
+    nudim_job_desc &d = jb->d;
+    jb->nmeas = (int)((d.gam_max - d.gam_min) / d.interval + 0.5) + 1;
+    jb->A = polar_lines(d.gam_min, d.interval, d.padangle, &jb->pad_min, &jb->pad_max);
+    jb->M = jb->A * d.np;
+    std::vector<double> x((size_t)jb->M * 2);
+    equal_angle_sample_2d(jb->pad_min, jb->pad_max, d.padangle, d.np, x.data());
+    if (build_nfft_tables(d.np, d.np, jb->M, x.data(), 16, 16, &jb->tabs) != 0) {
+        set_error("invalid NFFT geometry");
+        return NUDIM_EINVAL;
+    }
+    classify_lines(jb->pad_min, d.padangle, d.gam_min, d.gam_max, d.interval, jb->A, &jb->known,
+                   &jb->order);
+    for (int a = 0; a < jb->A; a++)
+        if (jb->known[a] && jb->order[a] >= jb->nmeas) {
+            set_error("tilt index out of range");
+            return NUDIM_EINVAL;
+        }
+    jb->unk_rank.assign(jb->M, 0);
+    int cnt = 0;
+    for (int i = 0; i < jb->M; i++) {
+        jb->unk_rank[i] = cnt;
+        if (!jb->known[i / d.np]) cnt++;
+    }
+    jb->n_unk_row = cnt;
+    if (d.precision == NUDIM_FP64) {
+        int rc = state_init<double>(jb.get(), jb->s64);
+        if (rc) {
+            jb->s64.release();
+            return rc;
+        }
+    } else {
+        int rc = state_init<float>(jb.get(), jb->s32);
+        if (!rc && d.correct_every > 0) rc = state_init<double>(jb.get(), jb->s64);
+        if (rc) {
+            jb->s32.release();
+            jb->s64.release();
+            return rc;
+        }
+    }
+    *out = jb.release();
+    return NUDIM_OK;
+}
+
+int nudim_job_destroy(nudim_job *jb)
+{
+    if (!jb) return NUDIM_OK;
+    cudaSetDevice(jb->ctx->device);
+    cudaStreamSynchronize(jb->ctx->stream);
+    jb->s64.release();
+    jb->s32.release();
+    delete jb;
+    return NUDIM_OK;
+}
+
+int nudim_job_import_fill(nudim_job *jb, const double *fill, size_t n)
+{
+    if (!jb || (!fill && n)) return NUDIM_EINVAL;
+    size_t need = (size_t)jb->n_unk_row * jb->d.nz;
+    if (n != need) {
+        set_error("fill has %zu values, the job has %zu unknown samples", n, need);
+        return NUDIM_EINVAL;
+    }
+    jb->fill.assign(fill, fill + n);
+    jb->fill_set = true;
+    return NUDIM_OK;
+}
+
+int nudim_job_set_projections(nudim_job *jb, const double *proj, size_t n)
+{
+    if (!jb || !proj) {
+        set_error("null argument");
+        return NUDIM_EINVAL;
+    }
+    const nudim_job_desc &d = jb->d;
+    size_t need = (size_t)jb->nmeas * d.nz * d.nx;
+    if (n != need) {
+        set_error("projections: got %zu values, need %d tilts x %d x %d = %zu", n, jb->nmeas, d.nz,
+                  d.nx, need);
+        return NUDIM_EINVAL;
+    }
+    nudim_ctx *ctx = jb->ctx;
+    NUDIM_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    // ---- tilt-series NFFT (reconstruction.c:307-367), FP64
+    int M1 = d.np * d.nz;
+    std::vector<double> x1((size_t)M1 * 2);
+    uniform_sample_2d(d.np, d.nz, x1.data());
+    NfftTables t1;
+    if (build_nfft_tables(d.nx, d.nz, M1, x1.data(), 16, 16, &t1) != 0) {
+        set_error("invalid tilt-series geometry (nx and nz must be even)");
+        return NUDIM_EINVAL;
+    }
+    NfftDev<double> p1;
+    int rc = p1.init(ctx, t1);
+    std::vector<void *> tmp;
+    auto talloc = [&](size_t b) -> void * {
+        void *q = nullptr;
+        if (cudaMalloc(&q, b) != cudaSuccess) return nullptr;
+        tmp.push_back(q);
+        return q;
+    };
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(st);
+        for (void *q : tmp) cudaFree(q);
+        p1.release();
+    };
+    double *d_proj = nullptr;
+    double2 *d_fh = nullptr, *d_tomo = nullptr;
+    int *d_order = nullptr, *d_rank = nullptr;
+    double *d_fill = nullptr;
+    if (!rc) {
+        d_proj = (double *)talloc(sizeof(double) * n);
+        d_fh = (double2 *)talloc(sizeof(double2) * n);
+        d_tomo = (double2 *)talloc(sizeof(double2) * (size_t)jb->nmeas * M1);
+        d_order = (int *)talloc(sizeof(int) * jb->A);
+        d_rank = (int *)talloc(sizeof(int) * jb->M);
+        if (!d_proj || !d_fh || !d_tomo || !d_order || !d_rank) {
+            set_error("out of device memory for the tilt series");
+            rc = NUDIM_ENOMEM;
+        }
+    }
+    if (!rc && d.random) {
+        size_t nf = (size_t)jb->n_unk_row * d.nz;
+        if (!jb->fill_set) {
+            jb->fill.resize(nf);
+            mt19937_uniform(0, nf, jb->fill.data());
+            for (double &v : jb->fill) v *= 10;  // gsl_rng_uniform(rng)*10
+        }
+        d_fill = (double *)talloc(sizeof(double) * (nf ? nf : 1));
+        if (!d_fill) rc = NUDIM_ENOMEM;
+        else if (nf) rc = cudaMemcpyAsync(d_fill, jb->fill.data(), sizeof(double) * nf,
+                                          cudaMemcpyHostToDevice, st) ? NUDIM_ECUDA : NUDIM_OK;
+    }
+    if (!rc) {
+        cudaMemcpyAsync(d_proj, proj, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(d_order, jb->order.data(), sizeof(int) * jb->A, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(d_rank, jb->unk_rank.data(), sizeof(int) * jb->M, cudaMemcpyHostToDevice,
+                        st);
+        k_proj_fhat<<<dim3(ceil_div((long)d.nx * d.nz, 256), jb->nmeas), 256, 0, st>>>(
+            d_proj, d_fh, d.nx, d.nz);
+        PadArgs<double> pa;
+        pa.src = d_fh;
+        pa.src_stride = (size_t)d.nx * d.nz;
+        InterpArgs<double> ia;
+        ia.out = d_tomo;
+        ia.out_stride = M1;
+        rc = p1.trafo(jb->nmeas, pa, ia, st);
+    }
+    // ---- reorder/mask/fill + initial inverse NFFT
+    if (!rc) {
+        if (d.precision == NUDIM_FP64)
+            rc = state_setup<double>(jb, jb->s64, d_tomo, d_order, d_rank, d_fill);
+        else {
+            rc = state_setup<float>(jb, jb->s32, d_tomo, d_order, d_rank, d_fill);
+            if (!rc && jb->s64.live)
+                rc = state_setup<double>(jb, jb->s64, d_tomo, d_order, d_rank, d_fill);
+        }
+    }
+    if (!rc) {
+        size_t V = (size_t)d.np * d.np * d.nz;
+        jb->vol0.resize(V);
+        rc = nudim_job_get_volume(jb, jb->vol0.data(), V, 0);
+    }
+    cleanup();
+    if (!rc) {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "set_projections", __FILE__, __LINE__);
+        jb->ready = true;
+        jb->done = 0;
+    }
+    return rc;
+}
+
+int nudim_step(nudim_ctx *ctx, nudim_job *const *jobs, int njobs, int iters)
+{
+    if (!ctx || (!jobs && njobs) || iters < 0) {
+        set_error("invalid nudim_step arguments");
+        return NUDIM_EINVAL;
+    }
+    NUDIM_CUDA(cudaSetDevice(ctx->device));
+    for (int it = 0; it < iters; it++) {
+        for (int k = 0; k < njobs; k++) {
+            nudim_job *jb = jobs[k];
+            if (!jb || jb->ctx != ctx) {
+                set_error("job %d does not belong to this context", k);
+                return NUDIM_EINVAL;
+            }
+            if (!jb->ready) {
+                set_error("nudim_step before nudim_job_set_projections");
+                return NUDIM_ESTATE;
+            }
+            int total = jb->d.nhio + jb->d.ner;
+            if (jb->done >= total) continue;
+            int nn = jb->done;
+            if (jb->d.precision == NUDIM_FP64) {
+                NUDIM_TRY(state_iterate<double>(jb, jb->s64, nn));
+            } else if (jb->d.correct_every > 0 && (nn + 1) % jb->d.correct_every == 0) {
+                NUDIM_TRY(corrective_iteration(jb, nn));
+            } else {
+                NUDIM_TRY(state_iterate<float>(jb, jb->s32, nn));
+            }
+            jb->done++;
+        }
+    }
+    return NUDIM_OK;
+}
+
+int nudim_job_get_volume(nudim_job *jb, double *out, size_t n, int crop)
+{
+    if (!jb || !out) return NUDIM_EINVAL;
+    const nudim_job_desc &d = jb->d;
+    size_t P2 = (size_t)d.np * d.np, V = P2 * d.nz;
+    size_t need = crop ? (size_t)d.nz * d.nx * d.nx : V;
+    if (n != need) {
+        set_error("volume buffer has %zu values, need %zu", n, need);
+        return NUDIM_EINVAL;
+    }
+    NUDIM_CUDA(cudaSetDevice(jb->ctx->device));
+    cudaStream_t st = jb->ctx->stream;
+    std::vector<double> full;
+    double *dst = crop ? (full.resize(V), full.data()) : out;
+    if (d.precision == NUDIM_FP64) {
+        NUDIM_CUDA(cudaMemcpyAsync(dst, jb->s64.img_a, sizeof(double) * V, cudaMemcpyDeviceToHost, st));
+    } else {
+        double *tmpd = (double *)jb->s32.z;  // V complex floats = V doubles of room
+        NUDIM_TRY(launch_to_double<float>(jb->s32.img_a, tmpd, V, st));
+        NUDIM_CUDA(cudaMemcpyAsync(dst, tmpd, sizeof(double) * V, cudaMemcpyDeviceToHost, st));
+    }
+    NUDIM_CUDA(cudaStreamSynchronize(st));
+    if (crop) {
+        int lo = (d.np - d.nx) / 2, hi = (d.np + d.nx) / 2;
+        size_t q = 0;
+        for (int i = 0; i < d.nz; i++)
+            for (int j = lo; j < hi; j++)
+                for (int k = lo; k < hi; k++) out[q++] = full[((size_t)i * d.np + j) * d.np + k];
+    }
+    return NUDIM_OK;
+}
+
+int nudim_job_get_initial_volume(nudim_job *jb, double *out, size_t n)
+{
+    if (!jb || !out) return NUDIM_EINVAL;
+    if (!jb->ready || jb->vol0.size() != n) {
+        set_error("initial volume unavailable or wrong size");
+        return jb->ready ? NUDIM_EINVAL : NUDIM_ESTATE;
+    }
+    memcpy(out, jb->vol0.data(), sizeof(double) * n);
+    return NUDIM_OK;
+}
+
+int nudim_job_get_rfactor(nudim_job *jb, double *hist, int cap, int *count)
+{
+    if (!jb || (!hist && cap > 0)) return NUDIM_EINVAL;
+    int n = std::min(cap, jb->done);
+    if (n > 0) {
+        NUDIM_CUDA(cudaSetDevice(jb->ctx->device));
+        NUDIM_CUDA(cudaStreamSynchronize(jb->ctx->stream));
+        double *src = jb->d.precision == NUDIM_FP64 ? jb->s64.rh : jb->s32.rh;
+        NUDIM_CUDA(cudaMemcpy(hist, src, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    }
+    if (count) *count = n;
+    return NUDIM_OK;
+}
+
+int nudim_job_iterations_done(nudim_job *jb, int *done)
+{
+    if (!jb || !done) return NUDIM_EINVAL;
+    *done = jb->done;
+    return NUDIM_OK;
+}
+
+int nudim_job_set_denoise_dump(nudim_job *jb, int nn, double *before, double *after)
+{
+    if (!jb) return NUDIM_EINVAL;
+    if (nn >= 0 && (!before || !after)) return NUDIM_EINVAL;
+    jb->dump_nn = nn;
+    jb->dump_before = before;
+    jb->dump_after = after;
+    return NUDIM_OK;
+}
+
+// ---------------------------------------------------------------- simulator
+int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, int nz, int np,
+                       double gam_min, double gam_max, double interval, double snr,
+                       unsigned long seed, double *proj_out, size_t n_out)
+{
+    if (!ctx || !density || !proj_out || nx <= 0 || ny <= 0 || nz <= 0 || np <= 0 ||
+        (nx | ny | nz | np) & 1 || !(interval > 0) || gam_min > gam_max || gam_min < -90 ||
+        gam_max > 90) {
+        set_error("invalid projection_sim arguments (sizes must be positive and even)");
+        return NUDIM_EINVAL;
+    }
+    int ns = equal_angle_count(gam_min, gam_max, interval);
+    if (n_out != (size_t)ns * nz * np) {
+        set_error("output has %zu values, need %d tilts x %d x %d", n_out, ns, nz, np);
+        return NUDIM_EINVAL;
+    }
+    NUDIM_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    int M = ns * np;
+    size_t XY = (size_t)nx * ny, V = XY * nz;
+    std::vector<double> x((size_t)M * 2);
+    equal_angle_sample_2d(gam_min, gam_max, interval, np, x.data());
+    NfftTables t;
+    build_nfft_tables(ny, nx, M, x.data(), 16, 16, &t);
+    NfftDev<double> pl;
+    int rc = pl.init(ctx, t);
+    double *dd = nullptr;
+    double2 *data = nullptr, *tmp = nullptr, *sl = nullptr;
+    if (!rc && (cudaMalloc(&dd, sizeof(double) * V) || cudaMalloc(&data, sizeof(double2) * V) ||
+                cudaMalloc(&tmp, sizeof(double2) * (size_t)nz * M) ||
+                cudaMalloc(&sl, sizeof(double2) * (size_t)ns * nz * np))) {
+        set_error("out of device memory in projection_sim");
+        rc = NUDIM_ENOMEM;
+    }
+    cufftHandle hz = 0, h2 = 0;
+    if (!rc) {
+        cudaMemcpyAsync(dd, density, sizeof(double) * V, cudaMemcpyHostToDevice, st);
+        k_real_cplx<<<ceil_div((long)V, 256), 256, 0, st>>>(dd, data, V);
+        int n1[1] = {nz};
+        // projection_sim.c:319-322: forward Z-FFT, stride nx*ny, unshifted
+        if (cufftPlanMany(&hz, 1, n1, n1, (int)XY, 1, n1, (int)XY, 1, CUFFT_Z2Z, (int)XY) ||
+            cufftSetStream(hz, st) ||
+            cufftExecZ2Z(hz, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data,
+                         CUFFT_FORWARD)) {
+            set_error("cuFFT failure in projection_sim Z-FFT");
+            rc = NUDIM_ECUDA;
+        }
+    }
+    if (!rc) {
+        // :325-351 per plane NFFT; plane q of `data` is slice (q + nz/2) % nz
+        PadArgs<double> pa;
+        pa.src = data;
+        pa.src_stride = XY;
+        InterpArgs<double> ia;
+        ia.out = tmp;
+        ia.out_stride = M;
+        rc = pl.trafo(nz, pa, ia, st);
+    }
+    if (!rc) {
+        // :359-374 ifftshift into slice[row][col], 2D backward FFT per tilt
+        k_sim_gather<<<dim3(ceil_div((long)nz * np, 256), ns), 256, 0, st>>>(tmp, sl, nz, np, M);
+        int n2[2] = {nz, np};
+        if (cufftPlanMany(&h2, 2, n2, nullptr, 1, nz * np, nullptr, 1, nz * np, CUFFT_Z2Z, ns) ||
+            cufftSetStream(h2, st) ||
+            cufftExecZ2Z(h2, (cufftDoubleComplex *)sl, (cufftDoubleComplex *)sl, CUFFT_INVERSE)) {
+            set_error("cuFFT failure in projection_sim 2D IFFT");
+            rc = NUDIM_ECUDA;
+        }
+    }
+    std::vector<double> host;
+    if (!rc) {
+        // :377-390 radial fftshift, keep the real part (scaled below)
+        k_sim_shift<<<dim3(ceil_div((long)nz * np, 256), ns), 256, 0, st>>>(sl, dd, nz, np);
+        host.resize((size_t)ns * nz * np);
+        cudaMemcpyAsync(host.data(), dd, sizeof(double) * host.size(), cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_fail(e, "projection_sim", __FILE__, __LINE__);
+    }
+    if (!rc) {
+        size_t per = (size_t)np * nz;
+        std::vector<double> u;
+        if (snr > 0) {
+            u.resize(2 * per * ns);
+            mt19937_uniform((uint32_t)seed, u.size(), u.data());
+        }
+        for (int j = 0; j < ns; j++) {
+            double *s = host.data() + (size_t)j * per;
+            if (snr > 0) {
+                // add_noise (projection_sim.c:45-67): sigma of Re(slice)
+                double sum = 0, sum2 = 0;
+                for (size_t i = 0; i < per; i++) {
+                    sum += s[i];
+                    sum2 += s[i] * s[i];
+                }
+                double sigma = sqrt(sum2 / per - (sum / per) * (sum / per)) / snr;
+                for (size_t i = 0; i < per; i++) {
+                    // Box-Muller on consecutive uniforms of the seeded stream
+                    size_t k = ((size_t)j * per + i);
+                    double u1 = u[2 * k], u2 = u[2 * k + 1];
+                    if (u1 <= 0) u1 = 1e-300;
+                    s[i] += sigma * sqrt(-2.0 * log(u1)) * cos(2.0 * kTruePi * u2);
+                }
+            }
+            for (size_t i = 0; i < per; i++) proj_out[(size_t)j * per + i] = s[i] / (np * nz);
+        }
+    }
+    if (hz) cufftDestroy(hz);
+    if (h2) cufftDestroy(h2);
+    cudaStreamSynchronize(st);
+    cudaFree(dd);
+    cudaFree(data);
+    cudaFree(tmp);
+    cudaFree(sl);
+    pl.release();
+    return rc;
+}
+
+// ---------------------------------------------------------------- operators
+int nudim_nfft_plan_create(nudim_ctx *ctx, int N0, int N1, int M, const double *x,
+                           int precision, nudim_nfft_plan **out)
+{
+    if (!ctx || !out || (!x && M) || M < 0 || (precision != 0 && precision != 1)) {
+        set_error("invalid plan arguments");
+        return NUDIM_EINVAL;
+    }
+    *out = nullptr;
+    for (long j = 0; j < 2L * M; j++)
+        if (!(x[j] >= -0.5 && x[j] < 0.5)) {
+            set_error("node coordinate %ld out of [-1/2, 1/2)", j);
+            return NUDIM_EINVAL;
+        }
+    NfftTables t;
+    if (build_nfft_tables(N0, N1, M, x, 16, 16, &t) != 0) {
+        set_error("N0 and N1 must be positive and even");
+        return NUDIM_EINVAL;
+    }
+    NUDIM_CUDA(cudaSetDevice(ctx->device));
+    auto *p = new nudim_nfft_plan();
+    p->ctx = ctx;
+    p->prec = precision;
+    int rc = precision == NUDIM_FP64 ? p->d64.init(ctx, t) : p->d32.init(ctx, t);
+    if (rc) {
+        p->d64.release();
+        p->d32.release();
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return NUDIM_OK;
+}
+
+int nudim_nfft_plan_destroy(nudim_nfft_plan *p)
+{
+    if (!p) return NUDIM_OK;
+    cudaSetDevice(p->ctx->device);
+    cudaDeviceSynchronize();
+    p->d64.release();
+    p->d32.release();
+    cudaFree(p->cg);
+    delete p;
+    return NUDIM_OK;
+}
+
+}  // extern "C"
+template <typename T>
+static int op_trafo(NfftDev<T> &d, int nplanes, const void *fh, void *f, cudaStream_t st)
+{
+    PadArgs<T> pa;
+    pa.src = fh;
+    pa.src_stride = (size_t)d.N0 * d.N1;
+    InterpArgs<T> ia;
+    ia.out = (cplx_t<T> *)f;
+    ia.out_stride = d.M;
+    return d.trafo(nplanes, pa, ia, st);
+}
+
+template <typename T>
+static int op_adjoint(NfftDev<T> &d, int nplanes, const void *f, void *fh, cudaStream_t st)
+{
+    SpreadArgs<T> sa;
+    sa.f = (const cplx_t<T> *)f;
+    sa.f_stride = d.M;
+    CropArgs<T> ca;
+    ca.out = (cplx_t<T> *)fh;
+    ca.out_stride = (size_t)d.N0 * d.N1;
+    return d.adjoint(nplanes, sa, ca, st);
+}
+
+extern "C" {
+int nudim_nfft_trafo(nudim_nfft_plan *p, int nplanes, const void *f_hat, void *f, void *stream)
+{
+    if (!p || nplanes < 0 || (nplanes && (!f_hat || !f))) return NUDIM_EINVAL;
+    NUDIM_CUDA(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->prec == NUDIM_FP64 ? op_trafo(p->d64, nplanes, f_hat, f, st)
+                                 : op_trafo(p->d32, nplanes, f_hat, f, st);
+}
+
+int nudim_nfft_adjoint(nudim_nfft_plan *p, int nplanes, const void *f, void *f_hat, void *stream)
+{
+    if (!p || nplanes < 0 || (nplanes && (!f_hat || !f))) return NUDIM_EINVAL;
+    NUDIM_CUDA(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->prec == NUDIM_FP64 ? op_adjoint(p->d64, nplanes, f, f_hat, st)
+                                 : op_adjoint(p->d32, nplanes, f, f_hat, st);
+}
+
+}  // extern "C"
+template <typename T>
+static int op_cgnr(nudim_nfft_plan *p, NfftDev<T> &d, int nplanes, const void *y, const void *w,
+                   void *f, int iters, cudaStream_t st)
+{
+    using C = cplx_t<T>;
+    size_t N = (size_t)d.N0 * d.N1, M = d.M;
+    int stride = cgnr_part_stride((int)M, (int)N);
+    size_t need = sizeof(C) * nplanes * (2 * M + 2 * N) +
+                  sizeof(double) * ((size_t)nplanes * (stride + 4) + 8);
+    if (need > p->cg_bytes) {
+        cudaDeviceSynchronize();
+        cudaFree(p->cg);
+        p->cg = nullptr;
+        p->cg_bytes = 0;
+        NUDIM_CUDA(cudaMalloc(&p->cg, need));
+        p->cg_bytes = need;
+    }
+    CgnrBuffers<T> b;
+    char *base = (char *)p->cg;
+    b.r = (C *)base;
+    b.v = b.r + nplanes * M;
+    b.z = b.v + nplanes * M;
+    b.p = b.z + nplanes * N;
+    b.part = (double *)(b.p + nplanes * N);
+    b.part_stride = stride;
+    b.dots = b.part + (size_t)nplanes * stride;
+    return cgnr_run<T>(d, nplanes, (const C *)y, (const T *)w, (C *)f, nullptr, false, iters, b,
+                       st);
+}
+
+extern "C" {
+int nudim_cgnr(nudim_nfft_plan *p, int nplanes, const void *y, const void *w, void *f_hat_iter,
+               int iters, void *stream)
+{
+    if (!p || nplanes < 0 || iters < 0 || (nplanes && (!y || !f_hat_iter))) return NUDIM_EINVAL;
+    if (!nplanes) return NUDIM_OK;
+    NUDIM_CUDA(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->prec == NUDIM_FP64 ? op_cgnr(p, p->d64, nplanes, y, w, f_hat_iter, iters, st)
+                                 : op_cgnr(p, p->d32, nplanes, y, w, f_hat_iter, iters, st);
+}
+
+int nudim_tv(nudim_ctx *ctx, int precision, void *vol, int nz, int ny, int nx, float lam,
+             int niter, int height, int nheight, int ncenter, void *stream)
+{
+    if (!ctx || !vol || nz <= 0 || ny <= 0 || nx <= 0 || niter < 0 ||
+        (precision != 0 && precision != 1)) {
+        set_error("invalid nudim_tv arguments");
+        return NUDIM_EINVAL;
+    }
+    NUDIM_CUDA(cudaSetDevice(ctx->device));
+    size_t V = (size_t)nz * ny * nx;
+    int cap = tv_part_count(nz, ny, nx);
+    size_t sT = precision == NUDIM_FP64 ? 8 : 4;
+    double *scr;
+    NUDIM_TRY(ctx_scratch(ctx, sizeof(double) * (cap + 4) + sT * V, &scr));
+    double *part = scr, *scal = scr + cap;
+    void *grad = (void *)(scr + cap + 4);
+    int ylo = (2 * ncenter - nheight) / 2, yhi = (2 * ncenter + nheight) / 2;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == NUDIM_FP64)
+        return tv_run<double>((double *)vol, (double *)grad, part, cap, scal, nz, ny, nx, lam,
+                              niter, height ? 1 : 0, ylo, yhi, st);
+    return tv_run<float>((float *)vol, (float *)grad, part, cap, scal, nz, ny, nx, lam, niter,
+                         height ? 1 : 0, ylo, yhi, st);
+}
+
+int nudim_diffusion2d(nudim_ctx *ctx, int precision, void *vol, int nz, int ny, int nx,
+                      int nx_bound, float lambda, float kappa, int niter, void *stream)
+{
+    if (!ctx || !vol || nz <= 0 || ny <= 0 || nx <= 0 || nx_bound <= 0 || niter < 0 ||
+        (precision != 0 && precision != 1)) {
+        set_error("invalid nudim_diffusion2d arguments");
+        return NUDIM_EINVAL;
+    }
+    NUDIM_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == NUDIM_FP64)
+        return diffusion_run<double>((double *)vol, nz, ny, nx, nx_bound, lambda, kappa, niter, st);
+    return diffusion_run<float>((float *)vol, nz, ny, nx, nx_bound, lambda, kappa, niter, st);
+}
+
+}  // extern "C"

@@ -1,0 +1,155 @@
+// engine.cuh -- device engine of the NUDIM reconstruction loop.
+//
+// Data layout in HBM (per job, precision T = double | float, C = complex T):
+//   img_a, img_b   V = nz*np*np reals, [z][y][x]   (current / previous volume)
+//   data           V complex, [q][y][x]: Z-frequency planes in FFT order;
+//                  doubles as the CGNR solution f of every plane
+//   y, r, v        nz*M complex: CGNR right-hand side, residual, A p
+//   z, p           V complex: CGNR normal residual and search direction
+//   slices         nz*M complex: measured / filled Fourier samples, stored
+//                  in the q order of `data` (plane q <-> slice (q+nz/2)%nz)
+//   grid workspace chunk*n0*n1 complex, owned by the context
+#pragma once
+
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+#include "tables.h"
+
+struct nudim_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void *ws = nullptr;          // shared oversampled-grid workspace
+    size_t ws_bytes = 0;
+    size_t grid_budget = 0;      // bytes a single NFFT pass may use for grids
+    std::map<std::tuple<int, int, int, int>, cufftHandle> fft2d;  // n0,n1,batch,prec
+    std::map<std::tuple<int, int, int, int>, cufftHandle> fftz;   // nz,P2,prec,kind
+    double *scratch = nullptr;   // small reduction workspace (operator-level calls)
+    size_t scratch_bytes = 0;
+};
+
+namespace nudim {
+
+int ctx_workspace(nudim_ctx *ctx, size_t bytes, void **p);
+int ctx_scratch(nudim_ctx *ctx, size_t bytes, double **p);
+int ctx_fft2d(nudim_ctx *ctx, int n0, int n1, int batch, int prec, cufftHandle *h);
+
+template <typename T> cufftType fft_c2c();
+template <> inline cufftType fft_c2c<double>() { return CUFFT_Z2Z; }
+template <> inline cufftType fft_c2c<float>() { return CUFFT_C2C; }
+template <typename T> int fft_exec(cufftHandle h, cplx_t<T> *io, int dir);
+
+template <typename T> constexpr int prec_of();
+template <> constexpr int prec_of<double>() { return NUDIM_FP64; }
+template <> constexpr int prec_of<float>() { return NUDIM_MIXED; }
+
+// ------------------------------------------------------------ epilogues
+enum PadMode { PM_COMPLEX = 0, PM_REAL_INIT = 1 };
+enum InterpMode { IM_PLAIN = 0, IM_RESID = 1, IM_DOTV = 2, IM_CONSTRAINT = 3 };
+enum CropMode { CM_PLAIN = 0, CM_DOT = 1, CM_INIT = 2 };
+
+template <typename T> struct PadArgs {
+    int mode = PM_COMPLEX;
+    const void *src = nullptr;     // plane p at src + p*src_stride elements
+    size_t src_stride = 0;
+    cplx_t<T> *f_init = nullptr;   // PM_REAL_INIT: complex copy of the real input
+    size_t f_stride = 0;
+};
+
+template <typename T> struct InterpArgs {
+    int mode = IM_PLAIN;
+    cplx_t<T> *out = nullptr;      // f (PLAIN/DOTV), r (RESID), y (CONSTRAINT)
+    size_t out_stride = 0;
+    const cplx_t<T> *y = nullptr;  // RESID: r = y - A f
+    size_t y_stride = 0;
+    const T *w = nullptr;          // DOTV: weights (nullptr = 1)
+    const cplx_t<T> *s = nullptr;  // CONSTRAINT: measured samples
+    size_t s_stride = 0;
+    const int *known = nullptr;    // CONSTRAINT: per polar line
+    int line_len = 1;
+    double *part = nullptr;        // per-block partial sums, plane p at part + p*part_stride
+    int part_stride = 0;
+};
+
+template <typename T> struct SpreadArgs {
+    const cplx_t<T> *f = nullptr;
+    size_t f_stride = 0;
+    const T *w = nullptr;          // nullptr: unweighted
+};
+
+template <typename T> struct CropArgs {
+    int mode = CM_PLAIN;
+    cplx_t<T> *out = nullptr;
+    size_t out_stride = 0;
+    cplx_t<T> *p_out = nullptr;    // CM_INIT: search direction p = z
+    double *part = nullptr;
+    int part_stride = 0;
+};
+
+// ------------------------------------------------------------ NFFT plan
+template <typename T> struct NfftDev {
+    using C = cplx_t<T>;
+    nudim_ctx *ctx = nullptr;
+    int N0 = 0, N1 = 0, n0 = 0, n1 = 0, M = 0;
+    int ty = 16, tx = 16, nty = 0, ntx = 0;
+    int2 *u = nullptr;
+    T *psi = nullptr;       // M x 2kW
+    T *c0 = nullptr, *c1 = nullptr;
+    int *tile_off = nullptr, *tile_nodes = nullptr;
+    size_t bytes = 0;
+
+    int init(nudim_ctx *c, const NfftTables &t);
+    void release();
+    int chunk_for(int nplanes) const;
+    int interp_blocks() const { return ceil_div(M, 256); }
+    int crop_blocks() const { return ceil_div((long)N0 * N1, 256); }
+    int trafo(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia, cudaStream_t st);
+    int adjoint(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca, cudaStream_t st);
+};
+
+// CGNR over `nplanes` planes (solver_before_loop + iters x loop_one_step).
+// f: planes of N0*N1 (start value in, result out), y/r/v: planes of M,
+// z/p: planes of N0*N1.  f_zero: the start value is zero (skips A f).
+// f_real: when non-null the start value is this real array (planes of
+// N0*N1) and f is overwritten with it first.
+template <typename T> struct CgnrBuffers {
+    cplx_t<T> *r = nullptr, *v = nullptr, *z = nullptr, *p = nullptr;
+    double *part = nullptr;   // nplanes * part_stride
+    int part_stride = 0;
+    double *dots = nullptr;   // nplanes * 4
+};
+
+template <typename T>
+int cgnr_run(NfftDev<T> &pl, int nplanes, const cplx_t<T> *y, const T *w, cplx_t<T> *f,
+             const T *f_real, bool f_zero, int iters, CgnrBuffers<T> &b, cudaStream_t st);
+
+int cgnr_part_stride(int M, int N);
+
+// ------------------------------------------------------------ volume ops
+template <typename T>
+int launch_pack(const T *img, cplx_t<T> *data, int nz, size_t P2, cudaStream_t st);
+template <typename T>
+int launch_unpack(const cplx_t<T> *data, T *img, int nz, size_t P2, cudaStream_t st);
+template <typename T>
+int launch_constraint(T *img, const T *img_last, int nz, int np, int nx, int hio, int height,
+                      int ylo, int yhi, cudaStream_t st);
+template <typename T>
+int launch_finish_r(const double *part, int nparts, int nplanes, int stride, double *rh,
+                    int nn, cudaStream_t st);
+template <typename T>
+int launch_real_to(const double *src, T *dst, size_t n, cudaStream_t st);
+template <typename T>
+int launch_to_double(const T *src, double *dst, size_t n, cudaStream_t st);
+
+// ------------------------------------------------------------ denoise
+template <typename T>
+int tv_run(T *u, T *grad, double *part, int part_cap, double *scal, int nz, int ny, int nx,
+           float lam, int niter, int height, int ylo, int yhi, cudaStream_t st);
+int tv_part_count(int nz, int ny, int nx);
+template <typename T>
+int diffusion_run(T *u, int nz, int ny, int nx, int nx_bound, float lambda, float kappa,
+                  int niter, cudaStream_t st);
+
+}  // namespace nudim

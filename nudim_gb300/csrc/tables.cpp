@@ -1,0 +1,219 @@
+// tables.cpp -- host FP64 tables of the NUDIM engine.  Compiled with
+// -ffp-contract=off so that x86-64 and aarch64 hosts build identical tables.
+#include "tables.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+
+namespace nudim {
+
+static constexpr int kM = 6;
+static constexpr int kW = 2 * kM + 2;
+
+int grid_size(int N)
+{
+    int p = 1;
+    while (p < N) p <<= 1;
+    return 2 * p;
+}
+
+int equal_angle_count(double amin, double amax, double ainterval)
+{
+    return (int)((amax - amin) / ainterval + 0.5) + 1;
+}
+
+// Radius by repeated addition of 1/nx starting at -1/2 - 1/nx, node
+// (r sin g, r cos g) with g in degrees and the truncated pi of grid.h.
+void equal_angle_sample_2d(double amin, double amax, double ainterval, int nx, double *x)
+{
+    int ns = equal_angle_count(amin, amax, ainterval);
+    double angle = amin - ainterval;
+    for (int s = 0; s < ns; s++) {
+        angle += ainterval;
+        double step = 1.0 / nx, r = -0.5 - step;
+        double sg = sin(angle / 180 * kRefPi), cg = cos(angle / 180 * kRefPi);
+        double *xs = x + (size_t)s * nx * 2;
+        for (int i = 0; i < nx; i++) {
+            r += step;
+            xs[2 * i + 0] = r * sg;
+            xs[2 * i + 1] = r * cg;
+        }
+    }
+}
+
+void uniform_sample_2d(int nx, int nz, double *x)
+{
+    double ix = 1.0 / nx, iz = 1.0 / nz, z0 = -0.5 - iz;
+    for (int j = 0; j < nz; j++) {
+        z0 += iz;
+        double x0 = -0.5 - ix;
+        for (int i = 0; i < nx; i++) {
+            x0 += ix;
+            x[2 * ((size_t)j * nx + i) + 0] = x0;
+            x[2 * ((size_t)j * nx + i) + 1] = z0;
+        }
+    }
+}
+
+int polar_lines(double gam_min, double interval, double padangle, double *pad_min,
+                double *pad_max)
+{
+    int ntmp = (int)((-90 - gam_min) / interval);
+    double lo = gam_min + ntmp * interval;
+    ntmp = (int)((90 - gam_min) / interval);
+    double hi = gam_min + ntmp * interval;
+    if (pad_min) *pad_min = lo;
+    if (pad_max) *pad_max = hi;
+    return equal_angle_count(lo, hi, padangle);
+}
+
+// Modified Bessel I0 by its power series (positive terms; accurate to a few
+// ulp for the arguments m*b < 40 used here).
+static double bessel_i0(double x)
+{
+    double q = 0.25 * x * x, term = 1.0, sum = 1.0;
+    for (int k = 1; k < 500; k++) {
+        term *= q / ((double)k * (double)k);
+        sum += term;
+        if (term < sum * 1e-18) break;
+    }
+    return sum;
+}
+
+// Kaiser-Bessel window of the published NFFT method at distance dn (grid
+// cells) from the node: sinh(b*sqrt(m^2-dn^2)) / (pi*sqrt(m^2-dn^2)),
+// continued analytically (sin branch) beyond the cut-off.
+static double kb_phi(double dn, double b)
+{
+    double a = (double)kM * kM - dn * dn;
+    if (a > 0) {
+        double s = sqrt(a);
+        return sinh(b * s) / (kTruePi * s);
+    }
+    if (a < 0) {
+        double s = sqrt(-a);
+        return sin(b * s) / (kTruePi * s);
+    }
+    return b / kTruePi;
+}
+
+// n * phi_hat(k) = I0(m * sqrt(b^2 - (2 pi k / n)^2)).
+static double kb_phi_hat(int k, int n, double b)
+{
+    double t = 2.0 * kTruePi * (double)k / (double)n;
+    return bessel_i0((double)kM * sqrt(b * b - t * t));
+}
+
+int build_nfft_tables(int N0, int N1, int M, const double *x, int ty, int tx, NfftTables *t)
+{
+    if (N0 <= 0 || N1 <= 0 || M < 0 || (N0 & 1) || (N1 & 1)) return -1;
+    t->N0 = N0;
+    t->N1 = N1;
+    t->M = M;
+    t->n0 = grid_size(N0);
+    t->n1 = grid_size(N1);
+    double b0 = kTruePi * (2.0 - 1.0 / ((double)t->n0 / (double)N0));
+    double b1 = kTruePi * (2.0 - 1.0 / ((double)t->n1 / (double)N1));
+    t->u0.assign(M, 0);
+    t->u1.assign(M, 0);
+    t->psi.assign((size_t)M * 2 * kW, 0.0);
+    for (int j = 0; j < M; j++) {
+        for (int d = 0; d < 2; d++) {
+            int n = d ? t->n1 : t->n0;
+            double b = d ? b1 : b0;
+            double xn = x[2 * (size_t)j + d] * (double)n;
+            int u = (int)floor(xn) - kM;
+            (d ? t->u1 : t->u0)[j] = u;
+            double *ps = t->psi.data() + (size_t)j * 2 * kW + (size_t)d * kW;
+            for (int s = 0; s < kW; s++) ps[s] = kb_phi(xn - (double)(u + s), b);
+        }
+    }
+    t->c0.resize(N0);
+    t->c1.resize(N1);
+    for (int k = 0; k < N0; k++) t->c0[k] = 1.0 / kb_phi_hat(k - N0 / 2, t->n0, b0);
+    for (int k = 0; k < N1; k++) t->c1[k] = 1.0 / kb_phi_hat(k - N1 / 2, t->n1, b1);
+
+    // tile lists for the atomic-free gather form of the adjoint
+    t->ty = std::min(ty, t->n0);
+    t->tx = std::min(tx, t->n1);
+    t->nty = t->n0 / t->ty;
+    t->ntx = t->n1 / t->tx;
+    int ntiles = t->nty * t->ntx;
+    std::vector<int> cnt(ntiles + 1, 0);
+    auto visit = [&](int j, auto &&fn) {
+        int rows[16], cols[16], nr = 0, nc = 0;
+        for (int s = 0; s < kW; s++) {
+            int r = ((t->u0[j] + s) & (t->n0 - 1)) / t->ty;
+            int c = ((t->u1[j] + s) & (t->n1 - 1)) / t->tx;
+            bool hr = false, hc = false;
+            for (int q = 0; q < nr; q++) hr |= rows[q] == r;
+            for (int q = 0; q < nc; q++) hc |= cols[q] == c;
+            if (!hr && nr < 16) rows[nr++] = r;
+            if (!hc && nc < 16) cols[nc++] = c;
+        }
+        for (int a = 0; a < nr; a++)
+            for (int c = 0; c < nc; c++) fn(rows[a] * t->ntx + cols[c]);
+    };
+    for (int j = 0; j < M; j++) visit(j, [&](int tile) { cnt[tile + 1]++; });
+    for (int i = 0; i < ntiles; i++) cnt[i + 1] += cnt[i];
+    t->tile_off = cnt;
+    t->tile_nodes.assign(cnt[ntiles], 0);
+    std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+    for (int j = 0; j < M; j++) visit(j, [&](int tile) { t->tile_nodes[pos[tile]++] = j; });
+    return 0;
+}
+
+void cgnr_weights(int A, int np, double padangle, double *w)
+{
+    double h = (double)(np / 2);
+    for (int a = 0; a < A; a++)
+        for (int i = 0; i < np; i++) {
+            if (i == np / 2)
+                w[(size_t)a * np + i] = kRefPi / (4 * A * (h * h));
+            else
+                w[(size_t)a * np + i] = padangle / 180 * kRefPi * abs(i - np / 2) / (h * h);
+        }
+}
+
+void classify_lines(double pad_min, double padangle, double gam_min, double gam_max,
+                    double interval, int A, std::vector<int> *known, std::vector<int> *order)
+{
+    known->assign(A, 0);
+    order->assign(A, 0);
+    for (int a = 0; a < A; a++) {
+        double angle = pad_min + a * padangle;
+        int span = (int)(interval / padangle + 0.5);
+        int seq = (int)((angle - gam_min) / padangle + 0.5);
+        if ((angle < gam_min) || (angle > gam_max) || (seq % span != 0)) continue;
+        if (abs((int)angle) < 1e-5) continue;  // cross-validation band (-1, 1)
+        (*known)[a] = 1;
+        (*order)[a] = (int)((angle - gam_min) / interval + 0.5);
+    }
+}
+
+void mt19937_uniform(uint32_t seed, size_t n, double *out)
+{
+    uint32_t mt[624];
+    int mti;
+    mt[0] = seed == 0 ? 4357u : seed;
+    for (mti = 1; mti < 624; mti++)
+        mt[mti] = 1812433253u * (mt[mti - 1] ^ (mt[mti - 1] >> 30)) + (uint32_t)mti;
+    for (size_t q = 0; q < n; q++) {
+        if (mti >= 624) {
+            for (int k = 0; k < 624; k++) {
+                uint32_t y = (mt[k] & 0x80000000u) | (mt[(k + 1) % 624] & 0x7fffffffu);
+                mt[k] = mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+            }
+            mti = 0;
+        }
+        uint32_t y = mt[mti++];
+        y ^= y >> 11;
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= y >> 18;
+        out[q] = (double)y / 4294967296.0;
+    }
+}
+
+}  // namespace nudim

@@ -1,0 +1,49 @@
+// tables.h -- host FP64 tables of the NUDIM engine (node geometry, Kaiser-
+// Bessel window, deconvolution factors, spreading tile lists, CGNR weights,
+// polar-line classification, the GSL-default random fill).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+namespace nudim {
+
+constexpr double kRefPi = 3.1415926;               // src/grid.h:11
+constexpr double kTruePi = 3.14159265358979323846; // NFFT window constants
+
+int grid_size(int N);  // n = 2 * next_pow2(N) (reconstruction.c:316, 390)
+
+// src/grid.c:84 / 78-97 / 100-133
+int equal_angle_count(double amin, double amax, double ainterval);
+void equal_angle_sample_2d(double amin, double amax, double ainterval, int nx, double *x);
+void uniform_sample_2d(int nx, int nz, double *x);
+// src/reconstruction.c:375-384
+int polar_lines(double gam_min, double interval, double padangle, double *pad_min,
+                double *pad_max);
+
+struct NfftTables {
+    int N0 = 0, N1 = 0, n0 = 0, n1 = 0, M = 0;
+    std::vector<int> u0, u1;          // first window index per node (may be < 0)
+    std::vector<double> psi;          // M x (2*kW): psi0[0..kW), psi1[0..kW)
+    std::vector<double> c0, c1;       // 1 / (n * phi_hat(k)), centred k
+    // spreading (adjoint) tile lists: node ids whose window touches each
+    // ty x tx tile of the n0 x n1 grid, ascending, CSR layout.
+    int ty = 16, tx = 16, nty = 0, ntx = 0;
+    std::vector<int> tile_off, tile_nodes;
+};
+
+int build_nfft_tables(int N0, int N1, int M, const double *x, int ty, int tx, NfftTables *t);
+
+// reconstruction.c:415-426 (--weight)
+void cgnr_weights(int A, int np, double padangle, double *w);
+
+// reconstruction.c:437-484: per polar line a, known[a] = 1 when the line is
+// a measured tilt outside the cross-validation band, order[a] = tilt index.
+void classify_lines(double pad_min, double padangle, double gam_min, double gam_max,
+                    double interval, int A, std::vector<int> *known, std::vector<int> *order);
+
+// gsl_rng_uniform with gsl_rng_default (MT19937, seed 0 -> 4357).
+void mt19937_uniform(uint32_t seed, size_t n, double *out);
+
+}  // namespace nudim

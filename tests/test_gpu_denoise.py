@@ -1,0 +1,68 @@
+"""TV, TV-height and 2D diffusion on the GPU against golden vectors from the
+reference's own denoise.c and against the oracle.  FP64: diffusion is
+bit-identical (no reductions); TV differs only through the order of its two
+global sums (tolerance 1e-12).  FP32: 1e-4."""
+import numpy as np
+import pytest
+
+from gpu_util import rdtype, rel, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def run_tv(ctx, nudim_built, vol, prec, lam, it, height=0, h=0, c=0):
+    import torch
+    d = to_dev(vol, rdtype(prec))
+    nudim_built.tv(ctx, d.data_ptr(), vol.shape, prec, lam, it, height, h, c)
+    torch.cuda.synchronize()
+    return d.cpu().numpy().astype(np.float64)
+
+
+def run_df(ctx, nudim_built, vol, prec, lam, kap, it, nxb):
+    import torch
+    d = to_dev(vol, rdtype(prec))
+    nudim_built.diffusion2d(ctx, d.data_ptr(), vol.shape, nxb, prec, lam, kap, it)
+    torch.cuda.synchronize()
+    return d.cpu().numpy().astype(np.float64)
+
+
+@pytest.mark.parametrize("n", range(3))
+def test_tv_golden(gpu_ctx, nudim_built, golden, n):
+    lam, it = golden["tv_%d_args" % n]
+    out = run_tv(gpu_ctx, nudim_built, golden["tv_%d_in" % n], 0, lam, int(it))
+    assert rel(out, golden["tv_%d_out" % n]) < 1e-12
+
+
+@pytest.mark.parametrize("n", range(3))
+def test_tv_height_golden(gpu_ctx, nudim_built, golden, n):
+    lam, it, h, c = golden["th_%d_args" % n]
+    out = run_tv(gpu_ctx, nudim_built, golden["th_%d_in" % n], 0, lam, int(it), 1, int(h), int(c))
+    assert rel(out, golden["th_%d_out" % n]) < 1e-12
+
+
+@pytest.mark.parametrize("n", range(4))
+def test_diffusion_golden_bitwise(gpu_ctx, nudim_built, golden, n):
+    lam, kap, it = golden["df_%d_args" % n]
+    v = golden["df_%d_in" % n]
+    out = run_df(gpu_ctx, nudim_built, v, 0, lam, kap, int(it), v.shape[0])
+    assert np.array_equal(out, golden["df_%d_out" % n])
+
+
+@pytest.mark.parametrize("shape,nxb", [((6, 20, 24), 6), ((30, 16, 16), 30), ((16, 40, 40), 16)])
+def test_diffusion_nz_ne_np_vs_oracle(gpu_ctx, orc, nudim_built, shape, nxb):
+    """nz != np: the reference's x-boundary quirk and the one-past-the-row
+    read (defined as 0.0 here and in the oracle)."""
+    rng = np.random.default_rng(sum(shape))
+    v = 0.01 * rng.standard_normal(shape)
+    out = run_df(gpu_ctx, nudim_built, v, 0, 0.25, 0.005, 30, nxb)
+    assert np.array_equal(out, orc.diffusion_2d(v, 0.25, 0.005, 30, nx_bound=nxb))
+    out32 = run_df(gpu_ctx, nudim_built, v, 1, 0.25, 0.005, 30, nxb)
+    assert rel(out32, out) < 1e-4
+
+
+def test_tv_fp32_and_large(gpu_ctx, orc, nudim_built):
+    rng = np.random.default_rng(2)
+    v = rng.standard_normal((24, 40, 36)) * 0.3
+    ref = orc.tv(v, 0.2, 40)
+    assert rel(run_tv(gpu_ctx, nudim_built, v, 0, 0.2, 40), ref) < 1e-12
+    assert rel(run_tv(gpu_ctx, nudim_built, v, 1, 0.2, 40), ref) < 1e-4

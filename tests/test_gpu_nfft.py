@@ -1,0 +1,91 @@
+"""NFFT trafo/adjoint and CGNR on the GPU against the CPU oracle and the
+NDFT.  Tolerances: FP64 1e-10 relative L2 (the bar for one trafo/adjoint),
+FP32 2e-5."""
+import numpy as np
+import pytest
+
+from gpu_util import cdtype, rel, to_dev
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(32, 32, "polar", 0), (64, 64, "polar", 0), (24, 40, "random", 0),
+         (20, 12, "uniform", 0), (32, 32, "polar", 1), (64, 64, "polar", 1)]
+
+
+def nodes(orc, N0, N1, kind, seed):
+    if kind == "polar":
+        return orc.polar_nodes(-60, 60, 3, 1, N0)
+    if kind == "uniform":
+        return orc.uniform_sample_2d(28, N1)
+    return np.random.default_rng(seed).uniform(-0.5, 0.5, (700, 2))
+
+
+@pytest.mark.parametrize("N0,N1,kind,prec", CASES)
+def test_trafo_adjoint_vs_oracle(gpu_ctx, orc, nudim_built, N0, N1, kind, prec):
+    import torch
+    rng = np.random.default_rng(N0 + 7 * N1 + prec)
+    x = nodes(orc, N0, N1, kind, N0)
+    M, B = len(x), 3
+    plan = nudim_built.NfftPlan(gpu_ctx, N0, N1, x, prec)
+    ref = orc.NFFT(N0, N1, x)
+    fh = rng.standard_normal((B, N0, N1)) + 1j * rng.standard_normal((B, N0, N1))
+    y = rng.standard_normal((B, M)) + 1j * rng.standard_normal((B, M))
+    fh_d, y_d = to_dev(fh, cdtype(prec)), to_dev(y, cdtype(prec))
+    f_d = torch.zeros((B, M), dtype=fh_d.dtype, device="cuda")
+    g_d = torch.zeros((B, N0, N1), dtype=fh_d.dtype, device="cuda")
+    plan.trafo(B, fh_d.data_ptr(), f_d.data_ptr())
+    plan.adjoint(B, y_d.data_ptr(), g_d.data_ptr())
+    torch.cuda.synchronize()
+    f, g = f_d.cpu().numpy(), g_d.cpu().numpy()
+    tol = 1e-10 if prec == 0 else 2e-5
+    for b in range(B):
+        assert rel(f[b], ref.trafo(fh[b])) < tol
+        assert rel(g[b], ref.adjoint(y[b])) < tol
+    if N0 <= 32:  # and against the direct sum
+        assert rel(f[0], orc.ndft_trafo(N0, N1, x, fh[0])) < max(tol, 5e-11)
+        assert rel(g[0], orc.ndft_adjoint(N0, N1, x, y[0])) < max(tol, 5e-11)
+    plan.close()
+
+
+@pytest.mark.parametrize("P,nz", [(128, 2), (384, 1)])
+def test_trafo_adjoint_benchmark_plane_sizes(gpu_ctx, orc, nudim_built, P, nz):
+    """One or two planes at the P of the benchmark configurations."""
+    import torch
+    rng = np.random.default_rng(P)
+    x = orc.polar_nodes(-60, 60, 3 if P == 128 else 2, 1, P)
+    plan = nudim_built.NfftPlan(gpu_ctx, P, P, x, 0)
+    ref = orc.NFFT(P, P, x)
+    fh = rng.standard_normal((nz, P, P)) + 1j * rng.standard_normal((nz, P, P))
+    y = rng.standard_normal((nz, len(x))) + 1j * rng.standard_normal((nz, len(x)))
+    fh_d, y_d = to_dev(fh, np.complex128), to_dev(y, np.complex128)
+    f_d = torch.zeros((nz, len(x)), dtype=torch.complex128, device="cuda")
+    g_d = torch.zeros((nz, P, P), dtype=torch.complex128, device="cuda")
+    plan.trafo(nz, fh_d.data_ptr(), f_d.data_ptr())
+    plan.adjoint(nz, y_d.data_ptr(), g_d.data_ptr())
+    torch.cuda.synchronize()
+    for b in range(nz):
+        assert rel(f_d[b].cpu().numpy(), ref.trafo(fh[b])) < 1e-10
+        assert rel(g_d[b].cpu().numpy(), ref.adjoint(y[b])) < 1e-10
+
+
+@pytest.mark.parametrize("weighted,prec", [(True, 0), (False, 0), (True, 1)])
+def test_cgnr_vs_oracle(gpu_ctx, orc, nudim_built, weighted, prec):
+    import torch
+    rng = np.random.default_rng(11)
+    P, B = 32, 4
+    x = orc.polar_nodes(-60, 60, 3, 1, P)
+    M = len(x)
+    plan = nudim_built.NfftPlan(gpu_ctx, P, P, x, prec)
+    ref = orc.NFFT(P, P, x)
+    y = rng.standard_normal((B, M)) + 1j * rng.standard_normal((B, M))
+    f0 = rng.standard_normal((B, P, P)) + 0j
+    w = rng.uniform(0.1, 1.0, M) if weighted else None
+    rdt = np.float64 if prec == 0 else np.float32
+    y_d, f_d = to_dev(y, cdtype(prec)), to_dev(f0, cdtype(prec))
+    w_d = to_dev(w, rdt) if weighted else None
+    plan.cgnr(B, y_d.data_ptr(), w_d.data_ptr() if weighted else None, f_d.data_ptr(), 10)
+    torch.cuda.synchronize()
+    f = f_d.cpu().numpy()
+    tol = 1e-9 if prec == 0 else 1e-4
+    for b in range(B):
+        assert rel(f[b], ref.cgnr(y[b], f0[b], w=w, iters=10)) < tol

@@ -1,0 +1,119 @@
+"""Full reconstruction jobs on the GPU against the CPU oracle (the
+restatement of src/reconstruction.c:304-719 and reconstruction-parallel.c).
+
+Bars (relative L2 over the full volume): plain FP64 form 1e-8 after the ER
+iterations (the reference's volume bar), initial volume 1e-9; HIO runs are
+compared over few iterations (HIO is discontinuous at u = 0, so rounding can
+flip voxels; parity is pinned on ER); mixed form 1e-4 (chosen-form bar)."""
+import numpy as np
+import pytest
+
+from gpu_util import rel, small_phantom
+
+pytestmark = pytest.mark.gpu
+
+
+def case_inputs(orc, n, nz, npx, gmin, gmax, step, seed=3):
+    vol = small_phantom(n, nz, seed)
+    proj = orc.project_2d1d(vol, npx, gmin, gmax, step)
+    rng = np.random.default_rng(seed)
+    return proj + 0.05 * proj.std() * rng.standard_normal(proj.shape)
+
+
+def run_gpu(ctx, nudim_built, proj, fill=None, **kw):
+    job = nudim_built.Job(ctx, **kw)
+    if fill is not None:
+        job.import_fill(fill)
+    job.set_projections(proj)
+    v0 = job.initial_volume()
+    job.step(kw.get("nhio", 0) + kw.get("ner", 0))
+    out = job.volume(), job.rfactor(), v0
+    job.close()
+    return out
+
+
+CASES = {
+    "er_tv_weight": dict(nx=32, nz=16, np=32, gam_min=-60, gam_max=60, interval=3,
+                         padangle=1, nhio=0, ner=20, denoise=1, weight=1),
+    "er_nodenoise": dict(nx=24, nz=16, np=32, gam_min=-45, gam_max=50, interval=5,
+                         padangle=1, nhio=0, ner=6, denoise=0, weight=0),
+    "er_diffusion_nz_ne_np": dict(nx=28, nz=12, np=32, gam_min=-60, gam_max=60, interval=2,
+                                  padangle=2, nhio=0, ner=4, denoise=2, weight=1),
+    "er_tv_height": dict(nx=32, nz=16, np=32, gam_min=-60, gam_max=60, interval=3,
+                         padangle=1, nhio=0, ner=4, denoise=1, height=1, nheight=12,
+                         ncenter=14),
+    "parallel_variant": dict(nx=32, nz=16, np=32, gam_min=-60, gam_max=60, interval=3,
+                             padangle=1, nhio=0, ner=4, denoise=2, height=1, nheight=10,
+                             variant=1),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_job_fp64_vs_oracle(gpu_ctx, orc, nudim_built, name):
+    kw = CASES[name]
+    proj = case_inputs(orc, kw["nx"], kw["nz"], kw["nx"], kw["gam_min"], kw["gam_max"],
+                       kw["interval"])
+    v, rh, v0 = run_gpu(gpu_ctx, nudim_built, proj, **kw)
+    o0, ov, orh = orc.reconstruct(proj, **kw)
+    assert rel(v0, o0) < 1e-9
+    assert rel(v, ov) < 1e-8
+    assert np.allclose(rh, orh, rtol=1e-8, atol=0)
+
+
+def test_job_hio_short(gpu_ctx, orc, nudim_built):
+    kw = dict(nx=32, nz=16, np=32, gam_min=-60, gam_max=60, interval=3, padangle=1, nhio=3,
+              ner=2, denoise=1, weight=1)
+    proj = case_inputs(orc, 32, 16, 32, -60, 60, 3)
+    v, rh, v0 = run_gpu(gpu_ctx, nudim_built, proj, **kw)
+    o0, ov, orh = orc.reconstruct(proj, **kw)
+    assert rel(v, ov) < 1e-6
+    assert np.allclose(rh, orh, rtol=1e-6)
+
+
+def test_job_random_fill(gpu_ctx, orc, nudim_built):
+    """--random: the library's MT19937 stream and an imported fill both match
+    the oracle's fill (10 * uniform in (z, node) order)."""
+    kw = dict(nx=24, nz=8, np=24, gam_min=-60, gam_max=60, interval=3, padangle=1, nhio=0,
+              ner=2, denoise=0, weight=1, random=1)
+    proj = case_inputs(orc, 24, 8, 24, -60, 60, 3)
+    v, rh, v0 = run_gpu(gpu_ctx, nudim_built, proj, **kw)
+    o0, ov, orh = orc.reconstruct(proj, **kw)
+    assert rel(v0, o0) < 1e-9 and rel(v, ov) < 1e-8
+    A, _, _ = orc.polar_lines(-60, 60, 3, 1)
+    nunk = int(np.sum(orc.build_slices(np.zeros((41, 24 * 8), complex), **{
+        k: kw[k] for k in ("nx", "nz", "np", "gam_min", "gam_max", "interval", "padangle")})[1]
+        == 0))
+    fill = np.random.default_rng(9).uniform(0, 10, nunk)
+    v, rh, v0 = run_gpu(gpu_ctx, nudim_built, proj, fill=fill, **kw)
+    o0, ov, orh = orc.reconstruct(proj, fill=fill, **kw)
+    assert rel(v0, o0) < 1e-9 and rel(v, ov) < 1e-8
+
+
+def test_job_mixed_vs_oracle(gpu_ctx, orc, nudim_built):
+    kw = dict(CASES["er_tv_weight"], ner=8)
+    proj = case_inputs(orc, 32, 16, 32, -60, 60, 3)
+    o0, ov, orh = orc.reconstruct(proj, **kw)
+    v, rh, v0 = run_gpu(gpu_ctx, nudim_built, proj, precision=1, **kw)
+    assert rel(v, ov) < 1e-4
+    vc, rhc, _ = run_gpu(gpu_ctx, nudim_built, proj, precision=1, correct_every=4, **kw)
+    assert rel(vc, ov) < 1e-4
+
+
+def test_job_crop_and_state(gpu_ctx, orc, nudim_built):
+    kw = dict(nx=20, nz=8, np=24, gam_min=-60, gam_max=60, interval=3, padangle=1, nhio=0,
+              ner=3, denoise=0)
+    proj = case_inputs(orc, 20, 8, 20, -60, 60, 3)
+    job = nudim_built.Job(gpu_ctx, **kw)
+    with pytest.raises(nudim_built.NudimError) as e:
+        job.step(1)
+    assert e.value.code == -5  # NUDIM_ESTATE: step before projections
+    with pytest.raises(nudim_built.NudimError):
+        job.set_projections(proj[:-1])  # wrong size
+    job.set_projections(proj)
+    job.step(2)
+    assert job.done() == 2
+    job.step(5)  # stops at nhio + ner
+    assert job.done() == 3
+    full, crop = job.volume(), job.volume(crop=True)
+    assert np.array_equal(crop, full[:, 2:22, 2:22])
+    job.close()
