@@ -1,0 +1,401 @@
+"""Benchmark of the NUDIM dual-space reconstruction loop on GB300.
+
+Metric: voxel-iterations per second = nz * np^2 * (outer HIO/ER iterations)
+/ wall time of the iteration loop (one "step" = one outer iteration of the
+whole volume: Z-FFT, 12 NFFT + 11 adjoint NFFT per Z-plane inside the
+constraint + 10-step CGNR, inverse Z-FFT, denoise, HIO/ER).
+
+Workload (default): the precision-form configuration, a 256^3 blob + shell
+phantom simulated to 61 tilts (-60..60 deg step 2) of 384 x 256 pixels at
+SNR 0.5, reconstructed at np = nx = 384, nz = 256, padangle 1, 50 HIO + 50
+ER, anisotropic-diffusion denoise.  `value` is the mixed form (FP32
+spreading/FFT/stencils, FP64 tables), inputs resident in HBM; `e2e` is the
+same metric through the C ABI with host buffers (tilt series in, volume out,
+setup included); `fp64_plain` is the FP64 form on the same job.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank runs an independent replica on its own GPU
+(the path has no cross-rank exchange): value = all ranks' voxel-iterations
+/ max rank time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+CFG = "cfg2"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+# ------------------------------------------------------------------ ranks
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws, backend):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v, device=None):
+    """Largest value over ranks (the slowest rank's time)."""
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, v, device=None):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ workload
+def workload_config():
+    from nudim_gb300.synth import CONFIGS
+    c = CONFIGS[CFG]
+    r = c["recon"]
+    return c, dict(r)
+
+
+def job_kwargs(r, precision):
+    import nudim_gb300 as ng
+    return dict(nx=r["nx"], nz=r["nz"], np=r["np"], gam_min=r["gam_min"], gam_max=r["gam_max"],
+                interval=r["interval"], padangle=r["padangle"], nhio=r["nhio"], ner=r["ner"],
+                denoise=r["denoise"], weight=r["weight"], precision=precision,
+                variant=ng.VARIANT_SERIAL)
+
+
+def stream_events(ctx):
+    import torch
+    st = torch.cuda.ExternalStream(ctx.stream)
+    return st, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def timed_steps(ctx, job, steps):
+    """Device time (ms) of `steps` outer iterations on the context stream."""
+    import torch
+    st, e0, e1 = stream_events(ctx)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(steps):
+        job.step(1)
+    e1.record(st)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def roofline_from_profile(prof, peak_gbs, peak_kind):
+    mine = {k: v for k, v in prof.items() if k not in ("fft2d", "zfft") and v[1] > 0}
+    total = sum(v[0] for v in prof.values())
+    top = max(mine, key=lambda k: mine[k][0])
+    ms, n, b = mine[top]
+    per_launch_s = ms / n / 1e3
+    achieved = (b / n) / per_launch_s / 1e9
+    shares = {k: round(v[0] / total, 4) for k, v in prof.items() if v[1] > 0}
+    return top, {
+        "bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak_gbs,
+        "unit": "GB/s", "frac": round(achieved / peak_gbs, 4), "traffic": None,
+        "algorithmic_bytes_per_launch": b / n, "avg_launch_ms": ms / n,
+        "peak_source": peak_kind}, shares
+
+
+def cpu_baseline_sample(proj, r, iters=1, threads=None):
+    """The oracle (CPU restatement, FP64) on a bounded sample of the same job:
+    `threads` Z-planes run the per-plane NFFT+CGNR work (one plane per host
+    thread), the volume phases (Z-FFTs, denoise, constraints) run on the
+    full volume; the plane phase is extrapolated linearly to nz planes."""
+    from oracle import orc
+    orc.build()
+    threads = threads or os.cpu_count() or 1
+    kw = dict(nx=r["nx"], nz=r["nz"], np=r["np"], gam_min=r["gam_min"], gam_max=r["gam_max"],
+              interval=r["interval"], padangle=r["padangle"], nhio=r["nhio"], ner=r["ner"],
+              denoise=r["denoise"], weight=r["weight"], nthreads=threads,
+              plane_limit=min(threads, r["nz"]))
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.time()
+    R = orc.Recon(proj, **kw)
+    t_setup = time.time() - t0
+    R.iterate(iters)
+    tp, tv = R.times()
+    R.close()
+    nplanes = kw["plane_limit"]
+    t_iter = (tp * r["nz"] / nplanes + tv) / iters
+    V = r["nz"] * r["np"] ** 2
+    return {"value": V / t_iter, "unit": "voxel-iters/s", "cores": threads, "kind": "port",
+            "sample": "%d outer iteration(s) of the same job; per-plane NFFT+CGNR on %d of %d "
+                      "Z-planes (one per thread) extrapolated linearly, volume phases on the "
+                      "full volume; setup %.1f s untimed" % (iters, nplanes, r["nz"], t_setup),
+            "s_per_iter": t_iter}
+
+
+# ------------------------------------------------------------------ arms
+def run_reference(args):
+    ws, rank, local = dist_env()
+    dist = init_dist(ws, "gloo")
+    if rank != 0:
+        barrier(dist)
+        return 0
+    import nudim_gb300 as ng
+    from nudim_gb300 import build as nb
+    from nudim_gb300.synth import add_noise, blob_phantom
+    from oracle import orc
+    c, r = workload_config()
+    # the tilt series is simulated by the oracle's own 2D1D restatement
+    orc.build()
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    vol = blob_phantom(seed=20261203, **c["phantom"])
+    s = c["sim"]
+    proj = add_noise(orc.project_2d1d(vol, s["np"], s["gam_min"], s["gam_max"], s["interval"]),
+                     s["snr"], 20261204)
+    kw = dict(nx=r["nx"], nz=r["nz"], np=r["np"], gam_min=r["gam_min"], gam_max=r["gam_max"],
+              interval=r["interval"], padangle=r["padangle"], nhio=r["nhio"], ner=r["ner"],
+              denoise=r["denoise"], weight=r["weight"], nthreads=threads,
+              plane_limit=min(threads, r["nz"]))
+    R = orc.Recon(proj, **kw)
+    R.iterate(args.warmup)
+    tp0, tv0 = R.times()
+    R.iterate(args.steps)
+    tp1, tv1 = R.times()
+    R.close()
+    n = kw["plane_limit"]
+    t_iter = ((tp1 - tp0) * r["nz"] / n + (tv1 - tv0)) / args.steps
+    V = r["nz"] * r["np"] ** 2
+    value = V / t_iter
+    line = {
+        "impl": "reference", "metric": "voxel-iters/s", "value": value, "unit": "voxel-iters/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_iter * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config_block(r),
+        "cpu_baseline": {"value": value, "unit": "voxel-iters/s", "cores": threads,
+                         "kind": "port",
+                         "sample": "each step: 1 outer iteration, per-plane NFFT+CGNR on %d of "
+                                   "%d Z-planes (one per thread) extrapolated linearly, volume "
+                                   "phases on the full volume" % (n, r["nz"])},
+        "e2e": {"value": value, "unit": "voxel-iters/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    barrier(dist)
+    return 0
+
+
+def config_block(r):
+    return {"workload": "precision-form job: 256^3 blob+shell phantom, 61 tilts -60..60 step 2, "
+                        "np=nx=384, nz=256, padangle 1, 50 HIO + 50 ER, anisotropic diffusion",
+            "nx": r["nx"], "np": r["np"], "nz": r["nz"], "tilts": 61, "polar_lines": 181,
+            "nfft_grid": 1024, "nhio": r["nhio"], "ner": r["ner"], "denoise": "DIFFUSION",
+            "cgnr_steps": 10, "parallelism": "replicas",
+            "l2": "inputs larger than L2: the Z-frequency volume alone is 302 MB (FP32 complex)"}
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = init_dist(ws, "nccl")
+    dev = torch.device("cuda", local)
+    import nudim_gb300 as ng
+    from nudim_gb300 import build as nb
+    from nudim_gb300.synth import MASTER_SEED, make_inputs
+    nb.build()
+    peaks, peak_kind = load_peaks()
+    c, r = workload_config()
+    V = r["nz"] * r["np"] ** 2
+    ctx = ng.Context(local)
+    vol, proj = make_inputs(ctx, CFG, seed=MASTER_SEED + rank)
+
+    # ---- mixed form, device resident (the headline `value`)
+    job = ng.Job(ctx, **job_kwargs(r, ng.MIXED))
+    job.set_projections(proj)
+    job.step(args.warmup)
+    ctx.sync()
+    vol_mixed_w = job.volume()
+    barrier(dist)
+    clocks = ClockSampler(local)
+    clocks.start()
+    n0 = ng.lib().nudim_launch_count()
+    ctx.profile(True)
+    ms = timed_steps(ctx, job, args.steps)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    launches = int(ng.lib().nudim_launch_count() - n0)
+    clk = clocks.stop()
+    ms_max = max_over_ranks(dist, ms, dev)
+    value = ws * V * args.steps / (ms_max / 1e3)
+    top, roof, shares = roofline_from_profile(prof, peaks.get("hbm_gbs", 6800.0), peak_kind)
+    job.close()
+
+    # ---- e2e through the C ABI: host tilt series in, host volume out
+    e2e = None
+    if not args.no_e2e:
+        torch.cuda.synchronize()
+        barrier(dist)
+        t0 = time.perf_counter()
+        job = ng.Job(ctx, **job_kwargs(r, ng.MIXED))
+        job.set_projections(proj)
+        job.step(args.steps)
+        out = job.volume()
+        t_e2e = time.perf_counter() - t0
+        job.close()
+        t_e2e = max_over_ranks(dist, t_e2e, dev)
+        e2e = {"value": ws * V * args.steps / t_e2e, "unit": "voxel-iters/s",
+               "h2d_bytes_per_step": int(proj.nbytes // args.steps),
+               "d2h_bytes_per_step": int(out.nbytes // args.steps),
+               "includes": "job setup (tilt-series NFFT, slice reorder, initial inverse NFFT)"}
+
+    # ---- FP64 plain form on the same job (fewer steps: it is the slow form)
+    v64 = ms64 = err = None
+    fp64_steps = max(1, args.fp64_steps)
+    if not args.no_fp64:
+        job = ng.Job(ctx, **job_kwargs(r, ng.FP64))
+        job.set_projections(proj)
+        job.step(args.warmup)
+        ctx.sync()
+        vol64_w = job.volume()
+        ms64 = timed_steps(ctx, job, fp64_steps)
+        job.close()
+        ms64 = max_over_ranks(dist, ms64, dev)
+        v64 = ws * V * fp64_steps / (ms64 / 1e3)
+        err = float(np.linalg.norm(vol_mixed_w - vol64_w) / np.linalg.norm(vol64_w))
+
+    line = {
+        "metric": "voxel-iters/s", "value": value, "unit": "voxel-iters/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded blob+shell phantom, GPU 2D1D tilt-series simulation, "
+                "Gaussian noise at SNR 0.5",
+        "config": config_block(r),
+        "form": "mixed (FP32 spreading/FFT/stencils, compensated gather, FP64 node/KB tables)",
+        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "kernel_time_share": shares,
+        "clocks": clk,
+    }
+    if v64 is not None:
+        line["fp64_plain"] = {"value": v64, "unit": "voxel-iters/s",
+                              "ms_per_step": ms64 / fp64_steps, "steps": fp64_steps}
+        line["mixed_over_fp64"] = value / v64
+        line["rel_l2_mixed_vs_fp64_after_warmup"] = err
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_sample(proj, r)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+    barrier(dist)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -92,6 +92,20 @@ int nudim_ctx_create(int device, unsigned flags, nudim_ctx **out);
 int nudim_ctx_destroy(nudim_ctx *ctx);
 /* CUDA stream (cudaStream_t) the context launches job work on. */
 void *nudim_ctx_stream(nudim_ctx *ctx);
+/* Tracing (no counterpart in the reference, which only prints MPI_Wtime
+ * totals, reconstruction-parallel.c:881-883): per-kernel-class CUDA-event
+ * timing of the context's launches.  enable != 0 starts timing and clears
+ * the totals; nudim_ctx_profile_read synchronises and returns, for kernel
+ * class k (0 .. nudim_profile_kernel_count()-1), the summed device time,
+ * the number of timed launches and the algorithmic bytes they move. */
+int nudim_ctx_profile(nudim_ctx *ctx, int enable);
+int nudim_ctx_profile_read(nudim_ctx *ctx, int k, double *total_ms, long long *launches,
+                           double *bytes);
+int nudim_profile_kernel_count(void);
+const char *nudim_profile_kernel_name(int k);
+/* Kernels launched by this library in this process so far. */
+unsigned long long nudim_launch_count(void);
+
 /* Bytes of device memory a job with this descriptor keeps resident. */
 int nudim_job_footprint(const nudim_job_desc *desc, size_t *bytes);
 

@@ -27,6 +27,11 @@ EXPORTS = [
     ("nudim_ctx_destroy", _ip, [_vp]),
     ("nudim_ctx_stream", _vp, [_vp]),
     ("nudim_ctx_sync", _ip, [_vp]),
+    ("nudim_ctx_profile", _ip, [_vp, _ip]),
+    ("nudim_ctx_profile_read", _ip, [_vp, _ip, _dp, C.POINTER(C.c_longlong), _dp]),
+    ("nudim_profile_kernel_count", _ip, []),
+    ("nudim_profile_kernel_name", C.c_char_p, [_ip]),
+    ("nudim_launch_count", C.c_ulonglong, []),
     ("nudim_job_footprint", _ip, [_vp, C.POINTER(_sz)]),
     ("nudim_job_create", _ip, [_vp, _vp, C.POINTER(_vp)]),
     ("nudim_job_destroy", _ip, [_vp]),
@@ -134,6 +139,18 @@ class Context:
     def step(self, jobs, iters):
         arr = (C.c_void_p * len(jobs))(*[j.h for j in jobs])
         _check(lib().nudim_step(self.h, arr, len(jobs), iters))
+
+    def profile(self, enable=True):
+        _check(lib().nudim_ctx_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        """{kernel class: (total_ms, launches, algorithmic bytes)}"""
+        out = {}
+        for k in range(lib().nudim_profile_kernel_count()):
+            ms, n, b = C.c_double(), C.c_longlong(), C.c_double()
+            _check(lib().nudim_ctx_profile_read(self.h, k, C.byref(ms), C.byref(n), C.byref(b)))
+            out[lib().nudim_profile_kernel_name(k).decode()] = (ms.value, n.value, b.value)
+        return out
 
     def close(self):
         if getattr(self, "h", None):

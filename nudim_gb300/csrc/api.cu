@@ -172,6 +172,8 @@ template <typename T> static int zfft(nudim_job *jb, JobState<T> &s, int dir)
     int P2 = jb->d.np * jb->d.np;
     NUDIM_TRY(zfft_plan(jb->ctx, jb->d.nz, P2, prec_of<T>(), &h));
     NUDIM_CUFFT(cufftSetStream(h, jb->ctx->stream));
+    ProfScope ps(jb->ctx, PK_ZFFT, jb->ctx->stream,
+                 2.0 * sizeof(cplx_t<T>) * (double)P2 * jb->d.nz);
     return fft_exec<T>(h, s.data, dir);
 }
 
@@ -261,7 +263,11 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
     int nz = d.nz, np = d.np, M = jb->M;
     size_t P2 = (size_t)np * np, V = P2 * nz;
     // :548-559 data[t] = img[(t+nz/2)%nz]; forward Z-FFT
-    NUDIM_TRY(launch_pack<T>(s.img_a, s.data, nz, P2, st));
+    const double sT = sizeof(T), sC = sizeof(cplx_t<T>);
+    {
+        ProfScope ps(jb->ctx, PK_VOLUME, st, (sT + sC) * (double)V);
+        NUDIM_TRY(launch_pack<T>(s.img_a, s.data, nz, P2, st));
+    }
     NUDIM_TRY(zfft<T>(jb, s, CUFFT_FORWARD));
     // :565-582 per plane: trafo, reciprocal constraint, R-factor partials
     PadArgs<T> pa;
@@ -284,7 +290,10 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
     NUDIM_TRY(cgnr_run<T>(s.pl, nz, s.y, s.w, s.data, s.img_a, false, iters_of(jb), b, st));
     // :607-621 backward Z-FFT, img = Re(shifted data)/nz
     NUDIM_TRY(zfft<T>(jb, s, CUFFT_INVERSE));
-    NUDIM_TRY(launch_unpack<T>(s.data, s.img_b, nz, P2, st));
+    {
+        ProfScope ps(jb->ctx, PK_VOLUME, st, (sT + sC) * (double)V);
+        NUDIM_TRY(launch_unpack<T>(s.data, s.img_b, nz, P2, st));
+    }
     // :624-669 denoise
     bool dump = (nn == jb->dump_nn) && jb->dump_before && d.denoise != NUDIM_DENOISE_NONE;
     if (dump) {
@@ -295,10 +304,12 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
     }
     if (d.denoise == NUDIM_DENOISE_DIFFUSION) {
         float lam = d.variant == NUDIM_VARIANT_PARALLEL ? 0.4f : 0.25f;
+        ProfScope ps(jb->ctx, PK_DIFFUSION, st, 2.0 * sT * (double)V);
         NUDIM_TRY(diffusion_run<T>(s.img_b, nz, np, np, nz, lam, 0.005f, 80, st));
     } else if (d.denoise == NUDIM_DENOISE_TV) {
         bool h = d.height && d.variant == NUDIM_VARIANT_SERIAL;
         int ylo = (2 * d.ncenter - d.nheight) / 2, yhi = (2 * d.ncenter + d.nheight) / 2;
+        ProfScope ps(jb->ctx, PK_TV, st, 40 * 5.0 * sT * (double)V);
         NUDIM_TRY(tv_run<T>(s.img_b, s.grad, s.tv_part, s.tv_cap, s.tv_scal, nz, np, np, 0.2f, 40,
                             h ? 1 : 0, ylo, yhi, st));
     }
@@ -317,6 +328,7 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
         ylo = (2 * d.ncenter - d.nheight) / 2;
         yhi = (2 * d.ncenter + d.nheight) / 2;
     }
+    ProfScope ps(jb->ctx, PK_VOLUME, st, 3.0 * sT * (double)V);
     NUDIM_TRY(launch_constraint<T>(s.img_b, s.img_a, nz, np, d.nx, nn < d.nhio ? 1 : 0,
                                    d.height ? 1 : 0, ylo, yhi, st));
     return NUDIM_OK;
@@ -451,6 +463,43 @@ int nudim_ctx_destroy(nudim_ctx *c)
 }
 
 void *nudim_ctx_stream(nudim_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int nudim_ctx_profile(nudim_ctx *c, int enable)
+{
+    if (!c) return NUDIM_EINVAL;
+    NUDIM_CUDA(cudaSetDevice(c->device));
+    prof_collect(c);
+    for (int k = 0; k < PK_COUNT; k++) {
+        c->prof_ms[k] = 0;
+        c->prof_n[k] = 0;
+        c->prof_bytes[k] = 0;
+    }
+    c->prof_on = enable != 0;
+    return NUDIM_OK;
+}
+
+int nudim_ctx_profile_read(nudim_ctx *c, int k, double *total_ms, long long *launches,
+                           double *bytes)
+{
+    if (!c || k < 0 || k >= PK_COUNT) return NUDIM_EINVAL;
+    NUDIM_CUDA(cudaSetDevice(c->device));
+    prof_collect(c);
+    if (total_ms) *total_ms = c->prof_ms[k];
+    if (launches) *launches = c->prof_n[k];
+    if (bytes) *bytes = c->prof_bytes[k];
+    return NUDIM_OK;
+}
+
+int nudim_profile_kernel_count(void) { return PK_COUNT; }
+
+const char *nudim_profile_kernel_name(int k)
+{
+    static const char *names[PK_COUNT] = {"pad",   "fft2d",  "interp", "spread", "crop",
+                                          "cgvec", "zfft",   "volume", "tv",     "diffusion"};
+    return (k >= 0 && k < PK_COUNT) ? names[k] : nullptr;
+}
+
+unsigned long long nudim_launch_count(void) { return g_launches; }
 
 int nudim_ctx_sync(nudim_ctx *c)
 {
@@ -786,11 +835,12 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
     build_nfft_tables(ny, nx, M, x.data(), 16, 16, &t);
     NfftDev<double> pl;
     int rc = pl.init(ctx, t);
-    double *dd = nullptr;
+    double *dd = nullptr, *dout = nullptr;  // density (V) and tilt series (ns*nz*np)
     double2 *data = nullptr, *tmp = nullptr, *sl = nullptr;
     if (!rc && (cudaMalloc(&dd, sizeof(double) * V) || cudaMalloc(&data, sizeof(double2) * V) ||
                 cudaMalloc(&tmp, sizeof(double2) * (size_t)nz * M) ||
-                cudaMalloc(&sl, sizeof(double2) * (size_t)ns * nz * np))) {
+                cudaMalloc(&sl, sizeof(double2) * (size_t)ns * nz * np) ||
+                cudaMalloc(&dout, sizeof(double) * (size_t)ns * nz * np))) {
         set_error("out of device memory in projection_sim");
         rc = NUDIM_ENOMEM;
     }
@@ -832,9 +882,10 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
     std::vector<double> host;
     if (!rc) {
         // :377-390 radial fftshift, keep the real part (scaled below)
-        k_sim_shift<<<dim3(ceil_div((long)nz * np, 256), ns), 256, 0, st>>>(sl, dd, nz, np);
+        k_sim_shift<<<dim3(ceil_div((long)nz * np, 256), ns), 256, 0, st>>>(sl, dout, nz, np);
         host.resize((size_t)ns * nz * np);
-        cudaMemcpyAsync(host.data(), dd, sizeof(double) * host.size(), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(host.data(), dout, sizeof(double) * host.size(), cudaMemcpyDeviceToHost,
+                        st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = cuda_fail(e, "projection_sim", __FILE__, __LINE__);
     }
@@ -870,6 +921,7 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
     if (h2) cufftDestroy(h2);
     cudaStreamSynchronize(st);
     cudaFree(dd);
+    cudaFree(dout);
     cudaFree(data);
     cudaFree(tmp);
     cudaFree(sl);

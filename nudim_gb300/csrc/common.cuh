@@ -32,7 +32,14 @@ int cufft_fail(cufftResult r, const char *what, const char *file, int line);
         int s_ = (call);                                                        \
         if (s_ != NUDIM_OK) return s_;                                          \
     } while (0)
-#define NUDIM_LAUNCH_CHECK() NUDIM_CUDA(cudaGetLastError())
+// Every kernel launch of the library is followed by this check, which also
+// counts the launch (nudim_launch_count).
+extern unsigned long long g_launches;
+#define NUDIM_LAUNCH_CHECK()                                                    \
+    do {                                                                        \
+        ++::nudim::g_launches;                                                  \
+        NUDIM_CUDA(cudaGetLastError());                                         \
+    } while (0)
 
 // ---------------------------------------------------------------- constants
 constexpr int kM = 6;            // NFFT cut-off (reconstruction.c:319, 393)

@@ -18,9 +18,38 @@
 #include "common.cuh"
 #include "tables.h"
 
+namespace nudim {
+// Kernel classes timed by the per-kernel CUDA-event profiler.
+enum ProfKernel {
+    PK_PAD = 0,     // deconvolve + pad into the oversampled grid
+    PK_FFT2D,       // cuFFT oversampled-grid FFT
+    PK_INTERP,      // window interpolation (trafo gather) + epilogue
+    PK_SPREAD,      // atomic-free spreading gather (adjoint)
+    PK_CROP,        // crop + deconvolve (adjoint) + epilogue
+    PK_CGVEC,       // CGNR vector updates and dot finishes
+    PK_ZFFT,        // cuFFT Z-axis FFT
+    PK_VOLUME,      // pack/unpack, HIO/ER constraint, R-factor
+    PK_TV,          // TV gradient + update
+    PK_DIFFUSION,   // 2D anisotropic diffusion wavefront
+    PK_COUNT
+};
+struct ProfRec {
+    int k;
+    cudaEvent_t a, b;
+    double bytes;
+};
+}  // namespace nudim
+
 struct nudim_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // per-kernel event timing (nudim_ctx_profile)
+    bool prof_on = false;
+    std::vector<nudim::ProfRec> prof_pending;
+    std::vector<cudaEvent_t> prof_pool;
+    double prof_ms[nudim::PK_COUNT] = {};
+    long long prof_n[nudim::PK_COUNT] = {};
+    double prof_bytes[nudim::PK_COUNT] = {};
     void *ws = nullptr;          // shared oversampled-grid workspace
     size_t ws_bytes = 0;
     size_t grid_budget = 0;      // bytes a single NFFT pass may use for grids
@@ -31,6 +60,19 @@ struct nudim_ctx {
 };
 
 namespace nudim {
+
+// Times the launches issued on `st` while it lives (one record per scope);
+// `bytes` is the algorithmic traffic the scope's launches move.
+struct ProfScope {
+    nudim_ctx *c;
+    int k;
+    cudaStream_t st;
+    double bytes;
+    cudaEvent_t a = nullptr;
+    ProfScope(nudim_ctx *c_, int k_, cudaStream_t st_, double bytes_);
+    ~ProfScope();
+};
+int prof_collect(nudim_ctx *c);
 
 int ctx_workspace(nudim_ctx *ctx, size_t bytes, void **p);
 int ctx_scratch(nudim_ctx *ctx, size_t bytes, double **p);

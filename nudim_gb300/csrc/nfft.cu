@@ -40,6 +40,55 @@ int cufft_fail(cufftResult r, const char *what, const char *file, int line)
     return r == CUFFT_ALLOC_FAILED ? NUDIM_ENOMEM : NUDIM_ECUDA;
 }
 
+unsigned long long g_launches = 0;
+
+// ================================================================ profiler
+static cudaEvent_t prof_event(nudim_ctx *c)
+{
+    if (!c->prof_pool.empty()) {
+        cudaEvent_t e = c->prof_pool.back();
+        c->prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+ProfScope::ProfScope(nudim_ctx *c_, int k_, cudaStream_t st_, double bytes_)
+    : c(c_), k(k_), st(st_), bytes(bytes_)
+{
+    if (c && c->prof_on) {
+        a = prof_event(c);
+        cudaEventRecord(a, st);
+    }
+}
+
+ProfScope::~ProfScope()
+{
+    if (!a) return;
+    cudaEvent_t b = prof_event(c);
+    cudaEventRecord(b, st);
+    c->prof_pending.push_back({k, a, b, bytes});
+    if (c->prof_pending.size() > 4096) prof_collect(c);
+}
+
+int prof_collect(nudim_ctx *c)
+{
+    for (auto &r : c->prof_pending) {
+        cudaEventSynchronize(r.b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        c->prof_ms[r.k] += ms;
+        c->prof_n[r.k] += 1;
+        c->prof_bytes[r.k] += r.bytes;
+        c->prof_pool.push_back(r.a);
+        c->prof_pool.push_back(r.b);
+    }
+    c->prof_pending.clear();
+    return NUDIM_OK;
+}
+
 // ================================================================ context helpers
 int ctx_workspace(nudim_ctx *ctx, size_t bytes, void **p)
 {
@@ -119,6 +168,7 @@ void launch_finish_sums(const double *part, int nparts, int nplanes, int stride_
 {
     k_finish_sums<<<dim3(nplanes, nsums), 256, 0, st>>>(part, nparts, stride_in, out,
                                                          out_stride);
+    ++g_launches;
 }
 
 // ================================================================ plan setup
@@ -374,6 +424,12 @@ k_crop(const cplx_t<T> *__restrict__ grid, int n0, int n1, int N0, int N1,
 }
 
 // ================================================================ drivers
+// Algorithmic bytes per launch (profiler): c = complex size, T = real size.
+//   pad    nb*c*(N0*N1 + n0*n1)             read coefficients, write grid
+//   fft2d  nb*c*2*n0*n1                      one read + one write of the grid
+//   interp M*(8+2kW*T) + nb*c*(n0*n1 + M)    node tables once, grid, output
+//   spread M*(8+2kW*T) + nb*c*(M + n0*n1)    node tables once, input, grid
+//   crop   nb*c*2*N0*N1                      read window of grid, write result
 template <typename T>
 int NfftDev<T>::trafo(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia,
                       cudaStream_t st)
@@ -384,29 +440,39 @@ int NfftDev<T>::trafo(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia
     NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (size_t)n0 * n1 * chunk, &wsv));
     C *grid = (C *)wsv;
     size_t cells = (size_t)n0 * n1;
+    const double c = sizeof(C), tab = (double)M * (8 + 2 * kW * sizeof(T));
     for (int p0 = 0; p0 < nplanes; p0 += chunk) {
         int nb = std::min(chunk, nplanes - p0);
-        dim3 gpad(ceil_div((long)cells, 256), nb);
-        if (pa.mode == PM_COMPLEX)
-            k_pad<T, PM_COMPLEX><<<gpad, 256, 0, st>>>(pa.src, pa.src_stride, N0, N1, n0, n1, c0,
-                                                       c1, p0, grid, nullptr, 0);
-        else
-            k_pad<T, PM_REAL_INIT><<<gpad, 256, 0, st>>>(pa.src, pa.src_stride, N0, N1, n0, n1,
-                                                         c0, c1, p0, grid, pa.f_init,
-                                                         pa.f_stride);
-        NUDIM_LAUNCH_CHECK();
-        cufftHandle h;
-        NUDIM_TRY(ctx_fft2d(ctx, n0, n1, nb, prec_of<T>(), &h));
-        NUDIM_CUFFT(cufftSetStream(h, st));
-        NUDIM_TRY(fft_exec<T>(h, grid, CUFFT_FORWARD));
-        dim3 gi(interp_blocks(), nb);
-        switch (ia.mode) {
-        case IM_PLAIN: k_interp<T, IM_PLAIN><<<gi, 256, 0, st>>>(grid, n0, n1, u, psi, M, p0, ia); break;
-        case IM_RESID: k_interp<T, IM_RESID><<<gi, 256, 0, st>>>(grid, n0, n1, u, psi, M, p0, ia); break;
-        case IM_DOTV: k_interp<T, IM_DOTV><<<gi, 256, 0, st>>>(grid, n0, n1, u, psi, M, p0, ia); break;
-        default: k_interp<T, IM_CONSTRAINT><<<gi, 256, 0, st>>>(grid, n0, n1, u, psi, M, p0, ia); break;
+        {
+            ProfScope ps(ctx, PK_PAD, st, nb * c * ((double)N0 * N1 + (double)cells));
+            dim3 gpad(ceil_div((long)cells, 256), nb);
+            if (pa.mode == PM_COMPLEX)
+                k_pad<T, PM_COMPLEX><<<gpad, 256, 0, st>>>(pa.src, pa.src_stride, N0, N1, n0, n1,
+                                                           c0, c1, p0, grid, nullptr, 0);
+            else
+                k_pad<T, PM_REAL_INIT><<<gpad, 256, 0, st>>>(pa.src, pa.src_stride, N0, N1, n0,
+                                                             n1, c0, c1, p0, grid, pa.f_init,
+                                                             pa.f_stride);
+            NUDIM_LAUNCH_CHECK();
         }
-        NUDIM_LAUNCH_CHECK();
+        {
+            ProfScope ps(ctx, PK_FFT2D, st, nb * c * 2.0 * (double)cells);
+            cufftHandle h;
+            NUDIM_TRY(ctx_fft2d(ctx, n0, n1, nb, prec_of<T>(), &h));
+            NUDIM_CUFFT(cufftSetStream(h, st));
+            NUDIM_TRY(fft_exec<T>(h, grid, CUFFT_FORWARD));
+        }
+        {
+            ProfScope ps(ctx, PK_INTERP, st, tab + nb * c * ((double)cells + M));
+            dim3 gi(interp_blocks(), nb);
+            switch (ia.mode) {
+            case IM_PLAIN: k_interp<T, IM_PLAIN><<<gi, 256, 0, st>>>(grid, n0, n1, u, psi, M, p0, ia); break;
+            case IM_RESID: k_interp<T, IM_RESID><<<gi, 256, 0, st>>>(grid, n0, n1, u, psi, M, p0, ia); break;
+            case IM_DOTV: k_interp<T, IM_DOTV><<<gi, 256, 0, st>>>(grid, n0, n1, u, psi, M, p0, ia); break;
+            default: k_interp<T, IM_CONSTRAINT><<<gi, 256, 0, st>>>(grid, n0, n1, u, psi, M, p0, ia); break;
+            }
+            NUDIM_LAUNCH_CHECK();
+        }
     }
     return NUDIM_OK;
 }
@@ -420,27 +486,38 @@ int NfftDev<T>::adjoint(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> 
     void *wsv;
     NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (size_t)n0 * n1 * chunk, &wsv));
     C *grid = (C *)wsv;
+    const double c = sizeof(C), cells = (double)n0 * n1,
+                 tab = (double)M * (8 + 2 * kW * sizeof(T));
     for (int p0 = 0; p0 < nplanes; p0 += chunk) {
         int nb = std::min(chunk, nplanes - p0);
-        dim3 gs(nty * ntx, nb);
-        if (sa.w)
-            k_spread<T, true><<<gs, ty * tx, 0, st>>>(sa, u, psi, tile_off, tile_nodes, n0, n1,
-                                                      ty, tx, ntx, p0, grid);
-        else
-            k_spread<T, false><<<gs, ty * tx, 0, st>>>(sa, u, psi, tile_off, tile_nodes, n0, n1,
-                                                       ty, tx, ntx, p0, grid);
-        NUDIM_LAUNCH_CHECK();
-        cufftHandle h;
-        NUDIM_TRY(ctx_fft2d(ctx, n0, n1, nb, prec_of<T>(), &h));
-        NUDIM_CUFFT(cufftSetStream(h, st));
-        NUDIM_TRY(fft_exec<T>(h, grid, CUFFT_INVERSE));
-        dim3 gc(crop_blocks(), nb);
-        switch (ca.mode) {
-        case CM_PLAIN: k_crop<T, CM_PLAIN><<<gc, 256, 0, st>>>(grid, n0, n1, N0, N1, c0, c1, p0, ca); break;
-        case CM_DOT: k_crop<T, CM_DOT><<<gc, 256, 0, st>>>(grid, n0, n1, N0, N1, c0, c1, p0, ca); break;
-        default: k_crop<T, CM_INIT><<<gc, 256, 0, st>>>(grid, n0, n1, N0, N1, c0, c1, p0, ca); break;
+        {
+            ProfScope ps(ctx, PK_SPREAD, st, tab + nb * c * ((double)M + cells));
+            dim3 gs(nty * ntx, nb);
+            if (sa.w)
+                k_spread<T, true><<<gs, ty * tx, 0, st>>>(sa, u, psi, tile_off, tile_nodes, n0,
+                                                          n1, ty, tx, ntx, p0, grid);
+            else
+                k_spread<T, false><<<gs, ty * tx, 0, st>>>(sa, u, psi, tile_off, tile_nodes, n0,
+                                                           n1, ty, tx, ntx, p0, grid);
+            NUDIM_LAUNCH_CHECK();
         }
-        NUDIM_LAUNCH_CHECK();
+        {
+            ProfScope ps(ctx, PK_FFT2D, st, nb * c * 2.0 * cells);
+            cufftHandle h;
+            NUDIM_TRY(ctx_fft2d(ctx, n0, n1, nb, prec_of<T>(), &h));
+            NUDIM_CUFFT(cufftSetStream(h, st));
+            NUDIM_TRY(fft_exec<T>(h, grid, CUFFT_INVERSE));
+        }
+        {
+            ProfScope ps(ctx, PK_CROP, st, nb * c * 2.0 * N0 * N1);
+            dim3 gc(crop_blocks(), nb);
+            switch (ca.mode) {
+            case CM_PLAIN: k_crop<T, CM_PLAIN><<<gc, 256, 0, st>>>(grid, n0, n1, N0, N1, c0, c1, p0, ca); break;
+            case CM_DOT: k_crop<T, CM_DOT><<<gc, 256, 0, st>>>(grid, n0, n1, N0, N1, c0, c1, p0, ca); break;
+            default: k_crop<T, CM_INIT><<<gc, 256, 0, st>>>(grid, n0, n1, N0, N1, c0, c1, p0, ca); break;
+            }
+            NUDIM_LAUNCH_CHECK();
+        }
     }
     return NUDIM_OK;
 }

@@ -120,9 +120,12 @@ int cgnr_run(NfftDev<T> &pl, int nplanes, const cplx_t<T> *y, const T *w, cplx_t
         launch_finish_sums(b.part, pl.interp_blocks(), nplanes, b.part_stride, b.dots + 2, 4, 1,
                            st);
         // alpha = |z|^2 / dot_v; f += alpha p; r -= alpha v
-        dim3 gu(ceil_div((long)N + M, 256), nplanes);
-        k_cg_update<T><<<gu, 256, 0, st>>>(f, b.p, b.r, b.v, b.dots, cur, N, M);
-        NUDIM_LAUNCH_CHECK();
+        {
+            ProfScope ps(pl.ctx, PK_CGVEC, st, 3.0 * sizeof(C) * ((double)N + M) * nplanes);
+            dim3 gu(ceil_div((long)N + M, 256), nplanes);
+            k_cg_update<T><<<gu, 256, 0, st>>>(f, b.p, b.r, b.v, b.dots, cur, N, M);
+            NUDIM_LAUNCH_CHECK();
+        }
         // z = A^H W r, |z|^2
         CropArgs<T> cz;
         cz.mode = CM_DOT;
@@ -135,9 +138,12 @@ int cgnr_run(NfftDev<T> &pl, int nplanes, const cplx_t<T> *y, const T *w, cplx_t
         launch_finish_sums(b.part, pl.crop_blocks(), nplanes, b.part_stride, b.dots + nxt, 4, 1,
                            st);
         // beta = |z'|^2/|z|^2; p = beta p + z'
-        dim3 gp(ceil_div(N, 256), nplanes);
-        k_cg_pupdate<T><<<gp, 256, 0, st>>>(b.p, b.z, b.dots, cur, nxt, N);
-        NUDIM_LAUNCH_CHECK();
+        {
+            ProfScope ps(pl.ctx, PK_CGVEC, st, 3.0 * sizeof(C) * (double)N * nplanes);
+            dim3 gp(ceil_div(N, 256), nplanes);
+            k_cg_pupdate<T><<<gp, 256, 0, st>>>(b.p, b.z, b.dots, cur, nxt, N);
+            NUDIM_LAUNCH_CHECK();
+        }
         cur = nxt;
     }
     return NUDIM_OK;

@@ -16,6 +16,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -161,16 +162,21 @@ void orc_fft_many(double *data_d, int n, int howmany, int stride, int dist, int 
     cplx *data = (cplx *)data_d;
     fft_tw T;
     fft_tw_init(&T, n, sign < 0 ? -1 : 1);
-    cplx *a = (cplx *)malloc(sizeof(cplx) * (size_t)n);
-    cplx *b = (cplx *)malloc(sizeof(cplx) * (size_t)n);
-    for (int h = 0; h < howmany; h++) {
-        cplx *base = data + (size_t)h * dist;
-        for (int t = 0; t < n; t++) a[t] = base[(size_t)t * stride];
-        fft_1d(a, b, n, &T);
-        for (int t = 0; t < n; t++) base[(size_t)t * stride] = b[t];
+    /* independent transforms: threads cannot change any result */
+#pragma omp parallel
+    {
+        cplx *a = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+        cplx *b = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+#pragma omp for schedule(static)
+        for (int h = 0; h < howmany; h++) {
+            cplx *base = data + (size_t)h * dist;
+            for (int t = 0; t < n; t++) a[t] = base[(size_t)t * stride];
+            fft_1d(a, b, n, &T);
+            for (int t = 0; t < n; t++) base[(size_t)t * stride] = b[t];
+        }
+        free(a);
+        free(b);
     }
-    free(a);
-    free(b);
     free(T.tw);
 }
 
@@ -336,7 +342,8 @@ static void ws_free(nfft_ws *w)
     free(w->b);
 }
 
-static inline int wrap(int l, int n) { return ((l % n) + n) % n; }
+/* index modulo the oversampled grid size (a power of two) */
+static inline int wrap(int l, int n) { return l & (n - 1); }
 
 /* nfft_trafo (reconstruction.c:361, 571): f_j = sum_k f_hat_k exp(-2 pi i k x_j).
  * D: deconvolve + place at k mod n; F: forward FFT; B: window interpolation. */
@@ -591,6 +598,10 @@ static void tv_core(const double *img, double *out, float lam, int niter, int NZ
     int jlo = (2 * ncenter - nheight) / 2, jhi = (2 * ncenter + nheight) / 2;
     while (niter--) {
         double tmp0 = 0;
+        /* The gradient of each voxel depends only on u, so it is computed in
+         * parallel; the global sum below keeps the reference's (k, j, i)
+         * order, so the result is bit-identical to the serial loops. */
+#pragma omp parallel for schedule(static)
         for (int k = 0; k < NX; k++) {
             int kp = (k == NX - 1) ? NX - 1 : k + 1;
             int km = (k == 0) ? 0 : k - 1;
@@ -622,10 +633,17 @@ static void tv_core(const double *img, double *out, float lam, int niter, int NZ
                                t8 / sqrt(eps + t7 * t7 + t8 * t8 + t9 * t9) -
                                t12 / sqrt(eps + t10 * t10 + t11 * t11 + t12 * t12);
                     grad[IDX(i, j, k)] = g;
-                    tmp0 += g * g;
                 }
             }
         }
+        for (int k = 0; k < NX; k++)
+            for (int j = 0; j < NY; j++) {
+                if (use_height && (j < jlo || j > jhi)) continue;
+                for (int i = 0; i < NZ; i++) {
+                    double g = grad[IDX(i, j, k)];
+                    tmp0 += g * g;
+                }
+            }
         double dA = 0;
         double tn = sqrt(tmp0);
         for (int k = 0; k < NX; k++)
@@ -672,8 +690,11 @@ void orc_aniso_diffusion_2d(const double *img, double *out, float lambda, float 
     double *u = out;
     memmove(u, img, sizeof(double) * V);
     double Ksq = (double)kappa * (double)kappa;
-    while (niter--) {
-        for (int k = 0; k < NZ; k++) {
+    /* planes are independent: running them on several threads keeps every
+     * plane's sequential Gauss-Seidel order and result */
+#pragma omp parallel for schedule(dynamic)
+    for (int k = 0; k < NZ; k++) {
+        for (int it = 0; it < niter; it++) {
             for (int j = 0; j < NY; j++) {
                 int jp = (j == NY - 1) ? NY - 1 : j + 1;
                 int jm = (j == 0) ? 0 : j - 1;
@@ -826,17 +847,42 @@ int orc_build_slices(const orc_recon_params *prm, const double *tomograms_d,
     return 0;
 }
 
-int orc_reconstruct(const orc_recon_params *prm, const double *proj, const double *fill,
-                    double *vol0_out, double *vol_out, double *rhist_out)
+/* Staged form of reconstruction.c:304-719: begin = setup and initial
+ * inverse (:304-540), iterate = outer HIO/ER iterations (:545-703). */
+struct orc_recon {
+    orc_recon_params prm;
+    int M, nplanes, iters, nthreads, done;
+    size_t PP, V;
+    orc_nfft *pl;
+    double *w;
+    cplx *slices, *data;
+    int *mask;
+    double *img, *img_last, *den, *d1, *d2;
+    double t_planes, t_volume;
+};
+
+static double wall(void)
+{
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return (double)clock() / CLOCKS_PER_SEC;
+#endif
+}
+
+orc_recon *orc_recon_begin(const orc_recon_params *prm, const double *proj, const double *fill)
 {
     int nx = prm->nx, nz = prm->nz, np = prm->np;
-    if (nx <= 0 || nz <= 0 || np <= 0 || (nz & 1) || (np & 1)) return -1;
+    if (nx <= 0 || nz <= 0 || np <= 0 || (nz & 1) || (np & 1)) return NULL;
+    orc_recon *R = (orc_recon *)calloc(1, sizeof(orc_recon));
+    R->prm = *prm;
     int nslices = (int)((prm->gam_max - prm->gam_min) / prm->interval + 0.5) + 1;
-    int iters = prm->cgnr_iters > 0 ? prm->cgnr_iters : 10;
-    int nthreads = prm->nthreads > 0 ? prm->nthreads : 1;
-    int nplanes = (prm->plane_limit > 0 && prm->plane_limit < nz) ? prm->plane_limit : nz;
-
+    R->iters = prm->cgnr_iters > 0 ? prm->cgnr_iters : 10;
+    R->nthreads = prm->nthreads > 0 ? prm->nthreads : 1;
+    R->nplanes = (prm->plane_limit > 0 && prm->plane_limit < nz) ? prm->plane_limit : nz;
     size_t PP = (size_t)np * np, V = PP * nz;
+    R->PP = PP;
+    R->V = V;
     int ntotal = np * nz;
     cplx *tomograms = (cplx *)malloc(sizeof(cplx) * (size_t)ntotal * nslices);
     orc_tilt_series_fourier(nx, nz, np, nslices, proj, (double *)tomograms);
@@ -845,47 +891,48 @@ int orc_reconstruct(const orc_recon_params *prm, const double *proj, const doubl
     int A = orc_polar_lines(prm->gam_min, prm->gam_max, prm->interval, prm->padangle,
                             &pad_min, &pad_max);
     int M = A * np;
+    R->M = M;
     double *x = (double *)malloc(sizeof(double) * 2 * (size_t)M);
     orc_equal_angle_sample_2d(pad_min, pad_max, prm->padangle, np, x);
-    orc_nfft *pl = orc_nfft_create(np, np, M, x);
+    R->pl = orc_nfft_create(np, np, M, x);
     free(x);
 
     /* reconstruction.c:415-426 */
-    double *w = NULL;
     if (prm->weight) {
-        w = (double *)malloc(sizeof(double) * (size_t)M);
+        R->w = (double *)malloc(sizeof(double) * (size_t)M);
         for (int j = 0; j < A; j++)
             for (int i = 0; i < np; i++) {
                 double h = (double)(np / 2);
                 if (i == np / 2)
-                    w[j * np + i] = REF_PI / (4 * A * (h * h));
+                    R->w[j * np + i] = REF_PI / (4 * A * (h * h));
                 else
-                    w[j * np + i] = prm->padangle / 180 * REF_PI * abs(i - np / 2) / (h * h);
+                    R->w[j * np + i] = prm->padangle / 180 * REF_PI * abs(i - np / 2) / (h * h);
             }
     }
-
-    cplx *slices = (cplx *)malloc(sizeof(cplx) * (size_t)M * nz);
-    int *mask = (int *)malloc(sizeof(int) * (size_t)M * nz);
-    orc_build_slices(prm, (double *)tomograms, fill, (double *)slices, mask);
+    R->slices = (cplx *)malloc(sizeof(cplx) * (size_t)M * nz);
+    R->mask = (int *)malloc(sizeof(int) * (size_t)M * nz);
+    orc_build_slices(prm, (double *)tomograms, fill, (double *)R->slices, R->mask);
     free(tomograms);
 
-    cplx *data = (cplx *)calloc(V, sizeof(cplx));
-    double *img = (double *)malloc(sizeof(double) * V);
-    double *img_last = (double *)malloc(sizeof(double) * V);
-    double *den = (double *)malloc(sizeof(double) * V);
+    R->data = (cplx *)calloc(V, sizeof(cplx));
+    R->img = (double *)malloc(sizeof(double) * V);
+    R->img_last = (double *)malloc(sizeof(double) * V);
+    R->den = (double *)malloc(sizeof(double) * V);
+    R->d1 = (double *)malloc(sizeof(double) * nz);
+    R->d2 = (double *)malloc(sizeof(double) * nz);
 
     /* reconstruction.c:495-518: initial inverse NFFT per plane */
-#pragma omp parallel num_threads(nthreads)
+    cplx *data = R->data;
+#pragma omp parallel num_threads(R->nthreads)
     {
         cg_ws c;
-        cg_init(&c, pl);
+        cg_init(&c, R->pl);
         cplx *f = (cplx *)malloc(sizeof(cplx) * PP);
 #pragma omp for schedule(dynamic)
-        for (int j = 0; j < nplanes; j++) {
+        for (int j = 0; j < R->nplanes; j++) {
             for (size_t i = 0; i < PP; i++) f[i] = 0.0;
-            cgnr_ws(pl, &c, slices + (size_t)j * M, w, f, iters, NULL);
-            for (size_t i = 0; i < PP; i++)
-                data[((size_t)j * PP + i + V / 2) % V] = f[i];
+            cgnr_ws(R->pl, &c, R->slices + (size_t)j * M, R->w, f, R->iters, NULL);
+            for (size_t i = 0; i < PP; i++) data[((size_t)j * PP + i + V / 2) % V] = f[i];
         }
         free(f);
         cg_free(&c);
@@ -894,13 +941,20 @@ int orc_reconstruct(const orc_recon_params *prm, const double *proj, const doubl
     orc_fft_many((double *)data, nz, (int)PP, (int)PP, 1, +1);
     for (int j = 0; j < nz; j++)
         for (size_t i = 0; i < PP; i++)
-            img[(size_t)((j + nz / 2) % nz) * PP + i] = creal(data[(size_t)j * PP + i]) / nz;
-    if (vol0_out) memcpy(vol0_out, img, sizeof(double) * V);
+            R->img[(size_t)((j + nz / 2) % nz) * PP + i] = creal(data[(size_t)j * PP + i]) / nz;
+    return R;
+}
 
-    double *d1 = (double *)malloc(sizeof(double) * nz);
-    double *d2 = (double *)malloc(sizeof(double) * nz);
-
-    for (int nn = 0; nn < prm->nhio + prm->ner; nn++) {
+int orc_recon_iterate(orc_recon *R, int n, double *rhist_out)
+{
+    const orc_recon_params *prm = &R->prm;
+    int nx = prm->nx, nz = prm->nz, np = prm->np, M = R->M;
+    size_t PP = R->PP, V = R->V;
+    cplx *data = R->data;
+    double *img = R->img, *img_last = R->img_last;
+    for (int q = 0; q < n && R->done < prm->nhio + prm->ner; q++) {
+        int nn = R->done;
+        double t0 = wall();
         /* :548-553 */
         for (int j = 0; j < nz; j++)
             for (size_t i = 0; i < PP; i++) {
@@ -909,24 +963,25 @@ int orc_reconstruct(const orc_recon_params *prm, const double *proj, const doubl
             }
         /* :556-559 */
         orc_fft_many((double *)data, nz, (int)PP, (int)PP, 1, -1);
+        double t1 = wall();
         /* :565-601 */
-#pragma omp parallel num_threads(nthreads)
+#pragma omp parallel num_threads(R->nthreads)
         {
             cg_ws c;
-            cg_init(&c, pl);
+            cg_init(&c, R->pl);
             cplx *fh = (cplx *)malloc(sizeof(cplx) * PP);
             cplx *ff = (cplx *)malloc(sizeof(cplx) * (size_t)M);
             cplx *y = (cplx *)malloc(sizeof(cplx) * (size_t)M);
 #pragma omp for schedule(dynamic)
             for (int j = 0; j < nz; j++) {
-                d1[j] = 0;
-                d2[j] = 0;
-                if (j >= nplanes) continue;
+                R->d1[j] = 0;
+                R->d2[j] = 0;
+                if (j >= R->nplanes) continue;
                 size_t base = ((size_t)j * PP + V / 2) % V;
                 for (size_t i = 0; i < PP; i++) fh[i] = data[base + i];
-                nfft_trafo_ws(pl, &c.nw, fh, ff);
-                const cplx *s = slices + (size_t)j * M;
-                const int *mk = mask + (size_t)j * M;
+                nfft_trafo_ws(R->pl, &c.nw, fh, ff);
+                const cplx *s = R->slices + (size_t)j * M;
+                const int *mk = R->mask + (size_t)j * M;
                 double a1 = 0, a2 = 0;
                 for (int i = 0; i < M; i++) {
                     if (mk[i] > 0.5) {
@@ -938,11 +993,11 @@ int orc_reconstruct(const orc_recon_params *prm, const double *proj, const doubl
                         y[i] = ff[i];
                     }
                 }
-                d1[j] = a1;
-                d2[j] = a2;
+                R->d1[j] = a1;
+                R->d2[j] = a2;
                 const double *wp = img + (size_t)((j + nz / 2) % nz) * PP;
                 for (size_t i = 0; i < PP; i++) fh[i] = wp[i];
-                cgnr_ws(pl, &c, y, w, fh, iters, NULL);
+                cgnr_ws(R->pl, &c, y, R->w, fh, R->iters, NULL);
                 for (size_t i = 0; i < PP; i++) data[base + i] = fh[i];
             }
             free(fh);
@@ -950,10 +1005,11 @@ int orc_reconstruct(const orc_recon_params *prm, const double *proj, const doubl
             free(y);
             cg_free(&c);
         }
+        double t2 = wall();
         double diff1 = 0, diff2 = 0;
         for (int j = 0; j < nz; j++) {
-            diff1 += d1[j];
-            diff2 += d2[j];
+            diff1 += R->d1[j];
+            diff2 += R->d2[j];
         }
         if (rhist_out) rhist_out[nn] = sqrt(diff1 / diff2);
         /* :607-621 */
@@ -962,18 +1018,19 @@ int orc_reconstruct(const orc_recon_params *prm, const double *proj, const doubl
         /* :624-669 (serial) / reconstruction-parallel.c:761-802 */
         if (prm->denoise == 2) {
             float lamd = prm->variant == 1 ? 0.4f : 0.25f;
-            orc_aniso_diffusion_2d(img, den, lamd, 0.005f, 80, nz, np, np, nz);
-            memcpy(img, den, sizeof(double) * V);
+            orc_aniso_diffusion_2d(img, R->den, lamd, 0.005f, 80, nz, np, np, nz);
+            memcpy(img, R->den, sizeof(double) * V);
         } else if (prm->denoise == 1) {
             if (prm->height && prm->variant == 0)
-                orc_tv_discrete_height(img, den, 0.2f, 40, nz, np, np, prm->nheight,
+                orc_tv_discrete_height(img, R->den, 0.2f, 40, nz, np, np, prm->nheight,
                                        prm->ncenter);
             else
-                orc_tv_discrete(img, den, 0.2f, 40, nz, np, np);
-            memcpy(img, den, sizeof(double) * V);
+                orc_tv_discrete(img, R->den, 0.2f, 40, nz, np, np);
+            memcpy(img, R->den, sizeof(double) * V);
         }
         /* :672-700 (serial) / reconstruction-parallel.c:805-833 */
         int hio = nn < prm->nhio;
+#pragma omp parallel for schedule(static)
         for (int j = 0; j < nz; j++)
             for (size_t i = 0; i < PP; i++) {
                 int yi = (int)(i / np), xi = (int)(i % np);
@@ -995,19 +1052,50 @@ int orc_reconstruct(const orc_recon_params *prm, const double *proj, const doubl
                     img[o] = hio ? img_last[o] - 0.9 * img[o] : 0;
                 }
             }
+        double t3 = wall();
+        R->t_planes += t2 - t1;
+        R->t_volume += (t1 - t0) + (t3 - t2);
+        R->done++;
     }
-    if (vol_out) memcpy(vol_out, img, sizeof(double) * V);
+    return R->done;
+}
 
-    free(d1);
-    free(d2);
-    free(data);
-    free(img);
-    free(img_last);
-    free(den);
-    free(slices);
-    free(mask);
-    free(w);
-    orc_nfft_destroy(pl);
+void orc_recon_volume(const orc_recon *R, double *out)
+{
+    memcpy(out, R->img, sizeof(double) * R->V);
+}
+
+void orc_recon_times(const orc_recon *R, double *t_planes, double *t_volume)
+{
+    if (t_planes) *t_planes = R->t_planes;
+    if (t_volume) *t_volume = R->t_volume;
+}
+
+void orc_recon_end(orc_recon *R)
+{
+    if (!R) return;
+    orc_nfft_destroy(R->pl);
+    free(R->w);
+    free(R->slices);
+    free(R->mask);
+    free(R->data);
+    free(R->img);
+    free(R->img_last);
+    free(R->den);
+    free(R->d1);
+    free(R->d2);
+    free(R);
+}
+
+int orc_reconstruct(const orc_recon_params *prm, const double *proj, const double *fill,
+                    double *vol0_out, double *vol_out, double *rhist_out)
+{
+    orc_recon *R = orc_recon_begin(prm, proj, fill);
+    if (!R) return -1;
+    if (vol0_out) orc_recon_volume(R, vol0_out);
+    orc_recon_iterate(R, prm->nhio + prm->ner, rhist_out);
+    if (vol_out) orc_recon_volume(R, vol_out);
+    orc_recon_end(R);
     return 0;
 }
 

@@ -98,6 +98,18 @@ int orc_reconstruct(const orc_recon_params *prm, const double *proj,
                     const double *fill, double *vol0_out, double *vol_out,
                     double *rhist_out);
 
+/* Staged form: begin = setup + initial inverse (reconstruction.c:304-540),
+ * iterate = n outer iterations (:545-703); times accumulate separately for
+ * the per-plane NFFT+CGNR phase and the volume phases (Z-FFTs, denoise,
+ * constraints). */
+typedef struct orc_recon orc_recon;
+orc_recon *orc_recon_begin(const orc_recon_params *prm, const double *proj,
+                           const double *fill);
+int orc_recon_iterate(orc_recon *R, int n, double *rhist_out);
+void orc_recon_volume(const orc_recon *R, double *out);
+void orc_recon_times(const orc_recon *R, double *t_planes, double *t_volume);
+void orc_recon_end(orc_recon *R);
+
 /* Individual stages, exported so tests can check intermediate arrays. */
 int orc_tilt_series_fourier(int nx, int nz, int np, int nslices, const double *proj,
                             double *tomograms);

@@ -75,6 +75,13 @@ def lib():
         L.orc_reconstruct.restype = C.c_int
         L.orc_reconstruct.argtypes = [C.POINTER(ReconParams), _dp, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p]
+        L.orc_recon_begin.restype = C.c_void_p
+        L.orc_recon_begin.argtypes = [C.POINTER(ReconParams), _dp, C.c_void_p]
+        L.orc_recon_iterate.restype = C.c_int
+        L.orc_recon_iterate.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_recon_volume.argtypes = [C.c_void_p, _dp]
+        L.orc_recon_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_recon_end.argtypes = [C.c_void_p]
         L.orc_tilt_series_fourier.argtypes = [C.c_int] * 4 + [_dp, _dp]
         L.orc_build_slices.argtypes = [C.POINTER(ReconParams), _dp, C.c_void_p, _dp, _ip]
         L.orc_project_2d1d.argtypes = [_dp] + [C.c_int] * 4 + [C.c_double] * 3 + [_dp]
@@ -305,3 +312,38 @@ def ref_lib():
         L.ref_uniform_sample_2D.argtypes = [C.c_int, C.c_int, _dp]
         _ref = L
     return _ref
+
+
+class Recon:
+    """Staged oracle reconstruction (used to time the CPU baseline)."""
+
+    def __init__(self, proj, fill=None, **kw):
+        self.p = make_params(**kw)
+        self._proj = _c(proj).reshape(-1)
+        fl = None if fill is None else _c(fill)
+        self._h = lib().orc_recon_begin(C.byref(self.p), self._proj,
+                                        None if fl is None else fl.ctypes.data)
+        if not self._h:
+            raise ValueError("orc_recon_begin failed")
+        self.rh = np.zeros(max(1, self.p.nhio + self.p.ner))
+
+    def iterate(self, n):
+        return lib().orc_recon_iterate(self._h, n, self.rh.ctypes.data)
+
+    def volume(self):
+        v = np.zeros(self.p.nz * self.p.np * self.p.np)
+        lib().orc_recon_volume(self._h, v)
+        return v.reshape(self.p.nz, self.p.np, self.p.np)
+
+    def times(self):
+        a, b = C.c_double(), C.c_double()
+        lib().orc_recon_times(self._h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().orc_recon_end(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -25,3 +25,9 @@ def small_phantom(n, nz, seed=3):
     from nudim_gb300.synth import blob_phantom
     return blob_phantom((nz, n, n), nblobs=6, radius=n * 0.3, sigma_range=(1.5, 3.0),
                         amp_range=(0.3, 1.0), seed=seed)
+
+
+def perturbed(a, eps, seed=1):
+    """a * (1 + eps * N(0,1)): the input perturbation used to measure how far
+    the oracle itself moves under rounding-sized changes."""
+    return a * (1.0 + eps * np.random.default_rng(seed).standard_normal(np.shape(a)))

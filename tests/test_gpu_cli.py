@@ -30,7 +30,7 @@ def test_cli_roundtrip(tmp_path, orc, nudim_built):
     proj = proj.reshape(41, 16, 32)
     assert np.abs(proj - orc.project_2d1d(vol, 32, -60, 60, 3)).max() < 1e-6
     args = ["--prefix=prj", "--pad=32", "--nx=32", "--nz=16", "--max=60", "--min=-60", "-t", "3",
-            "--padangle=1", "--nhio=0", "--ner=5", "--denoise", "--method=TV", "--print",
+            "--padangle=1", "--nhio=0", "--ner=5", "--denoise", "--method=DIFFUSION", "--print",
             "--weight"]
     r = subprocess.run([exe("reconstruction"), *args], cwd=tmp_path, capture_output=True,
                        text=True, timeout=300)
@@ -38,7 +38,7 @@ def test_cli_roundtrip(tmp_path, orc, nudim_built):
     lines = [l for l in r.stdout.splitlines() if l.startswith("Iteration:")]
     assert len(lines) == 5
     o0, ov, orh = orc.reconstruct(proj, nx=32, nz=16, np=32, gam_min=-60, gam_max=60,
-                                  interval=3, padangle=1, nhio=0, ner=5, denoise=1, weight=1)
+                                  interval=3, padangle=1, nhio=0, ner=5, denoise=2, weight=1)
     for nn, l in enumerate(lines):
         assert abs(float(l.split()[-1]) - orh[nn]) < 2e-6
     rec0 = np.loadtxt(tmp_path / "recovered-0.txt")

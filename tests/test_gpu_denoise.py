@@ -65,4 +65,9 @@ def test_tv_fp32_and_large(gpu_ctx, orc, nudim_built):
     v = rng.standard_normal((24, 40, 36)) * 0.3
     ref = orc.tv(v, 0.2, 40)
     assert rel(run_tv(gpu_ctx, nudim_built, v, 0, 0.2, 40), ref) < 1e-12
-    assert rel(run_tv(gpu_ctx, nudim_built, v, 1, 0.2, 40), ref) < 1e-4
+    # TV's normalised-gradient step amplifies rounding (d/dt t/sqrt(1e-8+t^2)
+    # reaches 1e4): FP32 is held to 10x the oracle's own change under a 1e-7
+    # relative perturbation of the input.
+    vp = v * (1 + 1e-7 * np.random.default_rng(3).standard_normal(v.shape))
+    floor = rel(orc.tv(vp, 0.2, 40), ref)
+    assert rel(run_tv(gpu_ctx, nudim_built, v, 1, 0.2, 40), ref) < max(1e-5, 10 * floor)

@@ -86,6 +86,13 @@ def test_cgnr_vs_oracle(gpu_ctx, orc, nudim_built, weighted, prec):
     plan.cgnr(B, y_d.data_ptr(), w_d.data_ptr() if weighted else None, f_d.data_ptr(), 10)
     torch.cuda.synchronize()
     f = f_d.cpu().numpy()
-    tol = 1e-9 if prec == 0 else 1e-4
     for b in range(B):
-        assert rel(f[b], ref.cgnr(y[b], f0[b], w=w, iters=10)) < tol
+        fo = ref.cgnr(y[b], f0[b], w=w, iters=10)
+        if prec == 0:
+            assert rel(f[b], fo) < 1e-9
+        else:
+            # FP32: within 10x of the oracle's own change under a 1e-7
+            # (single-precision sized) perturbation of the data
+            yp = y[b] * (1 + 1e-7 * np.random.default_rng(b).standard_normal(M))
+            floor = rel(ref.cgnr(yp, f0[b], w=w, iters=10), fo)
+            assert rel(f[b], fo) < max(1e-5, 10 * floor)
