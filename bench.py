@@ -142,11 +142,18 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ workload
+NZ_OVERRIDE = None  # --nz: fewer Z-planes, for small-case profiling only
+
+
 def workload_config():
+    import copy
+
     from nudim_gb300.synth import CONFIGS
-    c = CONFIGS[CFG]
-    r = c["recon"]
-    return c, dict(r)
+    c = copy.deepcopy(CONFIGS[CFG])
+    if NZ_OVERRIDE:
+        c["phantom"]["shape"] = (NZ_OVERRIDE,) + tuple(c["phantom"]["shape"][1:])
+        c["recon"]["nz"] = NZ_OVERRIDE
+    return c, dict(c["recon"])
 
 
 def job_kwargs(r, precision):
@@ -275,7 +282,9 @@ def run_reference(args):
 
 def config_block(r):
     return {"workload": "precision-form job: 256^3 blob+shell phantom, 61 tilts -60..60 step 2, "
-                        "np=nx=384, nz=256, padangle 1, 50 HIO + 50 ER, anisotropic diffusion",
+                        "np=nx=384, nz=%d, padangle 1, --weight, 50 HIO + 50 ER, anisotropic "
+                        "diffusion" % r["nz"],
+            "weight": bool(r["weight"]),
             "nx": r["nx"], "np": r["np"], "nz": r["nz"], "tilts": 61, "polar_lines": 181,
             "nfft_grid": 1024, "nhio": r["nhio"], "ner": r["ner"], "denoise": "DIFFUSION",
             "cgnr_steps": 10, "parallelism": "replicas",
@@ -389,9 +398,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--nz", type=int, default=0,
+                    help="override the number of Z-planes (small-case profiling only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    global NZ_OVERRIDE
+    NZ_OVERRIDE = args.nz or None
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -76,7 +76,7 @@ CONFIGS = {
                               sigma_range=(2, 12), amp_range=(0.1, 1.0), nshells=10),
                  sim=dict(np=384, gam_min=-60, gam_max=60, interval=2, snr=0.5),
                  recon=dict(nx=384, nz=256, np=384, gam_min=-60, gam_max=60, interval=2,
-                            padangle=1, nhio=50, ner=50, denoise=2, weight=0)),
+                            padangle=1, nhio=50, ner=50, denoise=2, weight=1)),
     "cfg5": dict(phantom=dict(shape=(256, 512, 512), nblobs=300, radius=200,
                               sigma_range=(2, 12), amp_range=(0.1, 1.0), nshells=10),
                  sim=dict(np=768, gam_min=-60, gam_max=60, interval=1, snr=0.3),

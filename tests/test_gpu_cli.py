@@ -42,7 +42,8 @@ def test_cli_roundtrip(tmp_path, orc, nudim_built):
     for nn, l in enumerate(lines):
         assert abs(float(l.split()[-1]) - orh[nn]) < 2e-6
     rec0 = np.loadtxt(tmp_path / "recovered-0.txt")
-    assert np.abs(rec0 - o0.ravel()).max() < 1e-9 * max(1.0, np.abs(o0).max())
+    # "%le" keeps 7 significant digits
+    assert np.allclose(rec0, o0.ravel(), rtol=1e-6, atol=1e-12)
     rec = np.loadtxt(tmp_path / "recovered.txt")
     assert rec.size == 16 * 32 * 32
     assert np.abs(rec - ov.ravel()).max() < 2e-6

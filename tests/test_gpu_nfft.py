@@ -77,9 +77,17 @@ def test_cgnr_vs_oracle(gpu_ctx, orc, nudim_built, weighted, prec):
     M = len(x)
     plan = nudim_built.NfftPlan(gpu_ctx, P, P, x, prec)
     ref = orc.NFFT(P, P, x)
-    y = rng.standard_normal((B, M)) + 1j * rng.standard_normal((B, M))
+    # data = A f_true + noise; weights = the reference's density compensation
+    # (reconstruction.c:415-426), which keeps the 10-step CGNR well conditioned
+    f_true = rng.uniform(0, 1, (B, P, P)) + 0j
+    y = np.stack([ref.trafo(f_true[b]) for b in range(B)])
+    y = y + 0.3 * np.abs(y).std() * (rng.standard_normal((B, M)) + 1j * rng.standard_normal((B, M)))
     f0 = rng.standard_normal((B, P, P)) + 0j
-    w = rng.uniform(0.1, 1.0, M) if weighted else None
+    A = M // P
+    i = np.arange(P)
+    wline = np.where(i == P // 2, 3.1415926 / (4 * A * (P // 2) ** 2),
+                     1.0 / 180 * 3.1415926 * np.abs(i - P // 2) / (P // 2) ** 2)
+    w = np.tile(wline, A) if weighted else None
     rdt = np.float64 if prec == 0 else np.float32
     y_d, f_d = to_dev(y, cdtype(prec)), to_dev(f0, cdtype(prec))
     w_d = to_dev(w, rdt) if weighted else None
