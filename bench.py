@@ -305,7 +305,7 @@ def run_ours(args):
     c, r = workload_config()
     V = r["nz"] * r["np"] ** 2
     ctx = ng.Context(local)
-    vol, proj = make_inputs(ctx, CFG, seed=MASTER_SEED + rank)
+    vol, proj = make_inputs(ctx, CFG, seed=MASTER_SEED + rank, cfg=c)
 
     # ---- mixed form, device resident (the headline `value`)
     job = ng.Job(ctx, **job_kwargs(r, ng.MIXED))

@@ -87,7 +87,11 @@ typedef struct nudim_job_desc {
 const char *nudim_last_error(void);
 int nudim_abi_version(void);
 
-/* Create a context on CUDA device `device`.  flags: reserved, pass 0. */
+/* Context flags. */
+#define NUDIM_CTX_GRID_NFFT 1u /* NFFT through an n0 x n1 grid in HBM + cuFFT (cross-check
+                                  path); the default keeps the grid on chip (fused) */
+
+/* Create a context on CUDA device `device`.  flags: 0 or NUDIM_CTX_* bits. */
 int nudim_ctx_create(int device, unsigned flags, nudim_ctx **out);
 int nudim_ctx_destroy(nudim_ctx *ctx);
 /* CUDA stream (cudaStream_t) the context launches job work on. */

@@ -123,10 +123,13 @@ def footprint(**kw):
     return b.value
 
 
+CTX_GRID_NFFT = 1  # NFFT through an HBM grid + cuFFT (cross-check path)
+
+
 class Context:
-    def __init__(self, device=0):
+    def __init__(self, device=0, flags=0):
         h = C.c_void_p()
-        _check(lib().nudim_ctx_create(device, 0, C.byref(h)))
+        _check(lib().nudim_ctx_create(device, flags, C.byref(h)))
         self.h = h
 
     @property

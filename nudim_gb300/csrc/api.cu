@@ -422,7 +422,6 @@ int nudim_abi_version(void) { return NUDIM_ABI_VERSION; }
 
 int nudim_ctx_create(int device, unsigned flags, nudim_ctx **out)
 {
-    (void)flags;
     if (!out) {
         set_error("null output pointer");
         return NUDIM_EINVAL;
@@ -444,6 +443,9 @@ int nudim_ctx_create(int device, unsigned flags, nudim_ctx **out)
     }
     const char *gb = getenv("NUDIM_GRID_BUDGET_MB");
     c->grid_budget = gb ? (size_t)atol(gb) << 20 : ((size_t)2 << 30);
+    const char *fb = getenv("NUDIM_FUSED_BUDGET_MB");
+    c->fused_budget = fb ? (size_t)atol(fb) << 20 : ((size_t)96 << 20);
+    c->use_fused = !(flags & NUDIM_CTX_GRID_NFFT);
     *out = c;
     return NUDIM_OK;
 }

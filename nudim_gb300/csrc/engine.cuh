@@ -53,6 +53,8 @@ struct nudim_ctx {
     void *ws = nullptr;          // shared oversampled-grid workspace
     size_t ws_bytes = 0;
     size_t grid_budget = 0;      // bytes a single NFFT pass may use for grids
+    size_t fused_budget = 0;     // bytes of row spectra + partials per fused pass (L2 sized)
+    bool use_fused = true;       // NFFT path: fused (default) or cuFFT grid path
     std::map<std::tuple<int, int, int, int>, cufftHandle> fft2d;  // n0,n1,batch,prec
     std::map<std::tuple<int, int, int, int>, cufftHandle> fftz;   // nz,P2,prec,kind
     double *scratch = nullptr;   // small reduction workspace (operator-level calls)
@@ -142,14 +144,34 @@ template <typename T> struct NfftDev {
     int *tile_off = nullptr, *tile_nodes = nullptr;
     size_t bytes = 0;
 
+    // fused path (nfft_fused.cu): no oversampled grid in HBM
+    bool fused = false;
+    int BC = 0, nblk = 0, smax = 0, rows = 4;
+    C *tw0 = nullptr, *tw1 = nullptr;
+    int *blk_off = nullptr, *ent = nullptr, *band_row = nullptr, *band_off = nullptr,
+        *band_node = nullptr;
+    unsigned char *nslots = nullptr;
+
     int init(nudim_ctx *c, const NfftTables &t);
     void release();
     int chunk_for(int nplanes) const;
     int interp_blocks() const { return ceil_div(M, 256); }
-    int crop_blocks() const { return ceil_div((long)N0 * N1, 256); }
+    int crop_blocks() const
+    {
+        return fused ? ceil_div(N0, rows) : ceil_div((long)N0 * N1, 256);
+    }
     int trafo(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia, cudaStream_t st);
     int adjoint(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca, cudaStream_t st);
+
+    int init_fused(const NfftTables &t);
+    void release_fused();
+    int fused_chunk(int nplanes) const;
+    int trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia, cudaStream_t st);
+    int adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca,
+                      cudaStream_t st);
 };
+
+constexpr int kFusedWarps = 16;  // warps (and spreading row bands) per column-block CTA
 
 // CGNR over `nplanes` planes (solver_before_loop + iters x loop_one_step).
 // f: planes of N0*N1 (start value in, result out), y/r/v: planes of M,

@@ -208,6 +208,7 @@ template <typename T> int NfftDev<T>::init(nudim_ctx *c, const NfftTables &t)
             sizeof(int) * (t.tile_off.size() + t.tile_nodes.size());
     // pageable uploads may still be in flight when cudaMemcpy returns
     NUDIM_CUDA(cudaDeviceSynchronize());
+    if (c->use_fused) return init_fused(t);
     return NUDIM_OK;
 }
 
@@ -223,6 +224,7 @@ template <typename T> void NfftDev<T>::release()
     psi = nullptr;
     c0 = c1 = nullptr;
     tile_off = tile_nodes = nullptr;
+    if (fused) release_fused();
 }
 
 template <typename T> int NfftDev<T>::chunk_for(int nplanes) const
@@ -435,6 +437,7 @@ int NfftDev<T>::trafo(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia
                       cudaStream_t st)
 {
     if (nplanes <= 0) return NUDIM_OK;
+    if (fused) return trafo_fused(nplanes, pa, ia, st);
     int chunk = chunk_for(nplanes);
     void *wsv;
     NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (size_t)n0 * n1 * chunk, &wsv));
@@ -482,6 +485,7 @@ int NfftDev<T>::adjoint(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> 
                         cudaStream_t st)
 {
     if (nplanes <= 0) return NUDIM_OK;
+    if (fused) return adjoint_fused(nplanes, sa, ca, st);
     int chunk = chunk_for(nplanes);
     void *wsv;
     NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (size_t)n0 * n1 * chunk, &wsv));

@@ -1,0 +1,581 @@
+// nfft_fused.cu -- the fused NFFT: the n0 x n1 oversampled grid never goes
+// to HBM.  The uniform FFT factorises into a row pass and a column pass:
+//
+//   trafo   K1 row pass:   deconvolve + zero-pad each of the N0 nonzero rows,
+//                          n1-point FFT in shared memory           -> H [N0][n1]
+//           K2 column pass: load BC columns of H, n0-point FFTs in shared
+//                          memory, Kaiser-Bessel interpolation partials of
+//                          the nodes whose window meets these columns (half-
+//                          warp per node, shuffle reduction)     -> partials
+//           K3 combine:    f_j = sum of the node's partials (fixed order) +
+//                          the CGNR / constraint epilogue
+//   adjoint K4 column pass: spread the nodes into BC columns in shared memory
+//                          (each warp owns a row band; nodes in ascending
+//                          order; compensated FP32 sums), n0-point inverse
+//                          FFTs, keep the N0 rows                 -> H'[N0][n1]
+//           K5 row pass:   n1-point inverse FFT, crop to N1, deconvolve +
+//                          epilogue (|z|^2 partials, p = z)
+//
+// No atomics: every output element has exactly one writer, and every sum
+// has a fixed order, so results are deterministic.
+#include "engine.cuh"
+
+namespace nudim {
+
+// ================================================================ smem FFT
+template <typename T>
+__device__ __forceinline__ cplx_t<T> cmul(cplx_t<T> a, cplx_t<T> b)
+{
+    return mkc<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// `cnt` FFTs of length n = 2^logn stored back to back in a; b is scratch of
+// the same size.  DIR = -1 forward (e^{-2 pi i}), +1 inverse; unnormalised.
+// Stockham autosort (radix 4, one radix-2 stage when logn is odd).  tw holds
+// e^{-2 pi i t/n}.  All threads of the block call it; returns the buffer that
+// holds the result.
+template <typename T, int DIR>
+__device__ cplx_t<T> *block_fft(cplx_t<T> *a, cplx_t<T> *b, int n, int logn, int cnt,
+                                const cplx_t<T> *__restrict__ tw)
+{
+    using C = cplx_t<T>;
+    const int nthr = blockDim.x, tid = threadIdx.x;
+    int Ns = 1;
+    if (logn & 1) {
+        const int half = n >> 1;
+        for (int q = tid; q < cnt * half; q += nthr) {
+            int s = q >> (logn - 1), j = q & (half - 1);
+            const C *x = a + (size_t)s * n;
+            C *y = b + (size_t)s * n;
+            C v0 = x[j], v1 = x[j + half];
+            y[2 * j] = mkc<T>(v0.x + v1.x, v0.y + v1.y);
+            y[2 * j + 1] = mkc<T>(v0.x - v1.x, v0.y - v1.y);
+        }
+        C *t = a;
+        a = b;
+        b = t;
+        Ns = 2;
+        __syncthreads();
+    }
+    const int quarter = n >> 2;
+    for (; Ns < n; Ns <<= 2) {
+        const int step = n / (4 * Ns);
+        for (int q = tid; q < cnt * quarter; q += nthr) {
+            int s = q >> (logn - 2), j = q & (quarter - 1);
+            const C *x = a + (size_t)s * n;
+            C *y = b + (size_t)s * n;
+            int k = j & (Ns - 1);
+            C v0 = x[j], v1 = x[j + quarter], v2 = x[j + 2 * quarter], v3 = x[j + 3 * quarter];
+            if (Ns > 1) {
+                C w1 = tw[k * step], w2 = tw[2 * k * step], w3 = tw[3 * k * step];
+                if (DIR > 0) {
+                    w1.y = -w1.y;
+                    w2.y = -w2.y;
+                    w3.y = -w3.y;
+                }
+                v1 = cmul<T>(v1, w1);
+                v2 = cmul<T>(v2, w2);
+                v3 = cmul<T>(v3, w3);
+            }
+            C a0 = mkc<T>(v0.x + v2.x, v0.y + v2.y), a1 = mkc<T>(v0.x - v2.x, v0.y - v2.y);
+            C a2 = mkc<T>(v1.x + v3.x, v1.y + v3.y), a3 = mkc<T>(v1.x - v3.x, v1.y - v3.y);
+            int o = (j - k) * 4 + k;
+            y[o] = mkc<T>(a0.x + a2.x, a0.y + a2.y);
+            y[o + 2 * Ns] = mkc<T>(a0.x - a2.x, a0.y - a2.y);
+            // forward: X1 = a1 - i a3, X3 = a1 + i a3; inverse: the other way
+            if (DIR < 0) {
+                y[o + Ns] = mkc<T>(a1.x + a3.y, a1.y - a3.x);
+                y[o + 3 * Ns] = mkc<T>(a1.x - a3.y, a1.y + a3.x);
+            } else {
+                y[o + Ns] = mkc<T>(a1.x - a3.y, a1.y + a3.x);
+                y[o + 3 * Ns] = mkc<T>(a1.x + a3.y, a1.y - a3.x);
+            }
+        }
+        C *t = a;
+        a = b;
+        b = t;
+        __syncthreads();
+    }
+    return a;
+}
+
+
+// ================================================================ K1 row pass (trafo)
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256)
+k_rowfft(const void *__restrict__ src, size_t src_stride, int N0, int N1, int n1, int logn1,
+         int kRows, const T *__restrict__ c0, const T *__restrict__ c1,
+         const cplx_t<T> *__restrict__ tw1, int plane0, cplx_t<T> *__restrict__ H,
+         cplx_t<T> *__restrict__ f_init, size_t f_stride)
+{
+    using C = cplx_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *A = (C *)smraw, *B = A + kRows * n1;
+    int b = blockIdx.y, gb = plane0 + b, a0 = blockIdx.x * kRows;
+    int nr = min(kRows, N0 - a0);
+    for (int idx = threadIdx.x; idx < nr * n1; idx += blockDim.x) {
+        int r = idx / n1, l1 = idx - r * n1;
+        int k1 = l1 < n1 / 2 ? l1 : l1 - n1;
+        C v = mkc<T>(0, 0);
+        if (k1 >= -N1 / 2 && k1 < N1 / 2) {
+            int a = a0 + r, c = k1 + N1 / 2;
+            size_t o = (size_t)gb * src_stride + (size_t)a * N1 + c;
+            C s;
+            if (MODE == PM_COMPLEX) {
+                s = ((const C *)src)[o];
+            } else {
+                s = mkc<T>(((const T *)src)[o], T(0));
+                f_init[(size_t)gb * f_stride + (size_t)a * N1 + c] = s;
+            }
+            T sc = c0[a] * c1[c];
+            v = mkc<T>(s.x * sc, s.y * sc);
+        }
+        A[idx] = v;
+    }
+    __syncthreads();
+    C *R = block_fft<T, -1>(A, B, n1, logn1, nr, tw1);
+    C *Hb = H + ((size_t)b * N0 + a0) * n1;
+    for (int idx = threadIdx.x; idx < nr * n1; idx += blockDim.x) Hb[idx] = R[idx];
+}
+
+// ================================================================ K2 column pass + interpolation
+template <typename T>
+__global__ void __launch_bounds__(512)
+k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int n1, int BC,
+                const cplx_t<T> *__restrict__ tw0, const int2 *__restrict__ u,
+                const T *__restrict__ psi, const int *__restrict__ blk_off,
+                const int *__restrict__ ent, int M, int smax, cplx_t<T> *__restrict__ part)
+{
+    using C = cplx_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *A = (C *)smraw, *B = A + (size_t)BC * n0;
+    int cb = blockIdx.x, b = blockIdx.y;
+    const C *Hb = H + (size_t)b * N0 * n1 + (size_t)cb * BC;
+    // rows a of H land at l0 = (a - N0/2) mod n0; the other rows are zero
+    for (int idx = threadIdx.x; idx < n0 * BC; idx += blockDim.x) {
+        int l0 = idx / BC, c = idx - l0 * BC;
+        int k0 = l0 < n0 / 2 ? l0 : l0 - n0;
+        C v = mkc<T>(0, 0);
+        if (k0 >= -N0 / 2 && k0 < N0 / 2) v = Hb[(size_t)(k0 + N0 / 2) * n1 + c];
+        A[(size_t)c * n0 + l0] = v;
+    }
+    __syncthreads();
+    C *G = block_fft<T, -1>(A, B, n0, logn0, BC, tw0);
+    // half-warp per (node, block) entry
+    int lane = threadIdx.x & 31, t0 = lane & 15;
+    int hw = threadIdx.x >> 4, nhw = blockDim.x >> 4;
+    int beg = blk_off[cb], end = blk_off[cb + 1];
+    int col0 = cb * BC;
+    for (int e0 = beg; e0 < end; e0 += nhw) {
+        int e = e0 + hw;
+        T ar = 0, ai = 0;
+        int j = 0, slot = 0;
+        bool valid = e < end;
+        if (valid) {
+            int en = ent[e];
+            j = en >> 3;
+            slot = en & 7;
+            if (t0 < kW) {
+                int2 uu = u[j];
+                const T *ps = psi + (size_t)j * 2 * kW;
+                int r = (uu.x + t0) & (n0 - 1);
+#pragma unroll
+                for (int t1 = 0; t1 < kW; t1++) {
+                    int cl = ((uu.y + t1) & (n1 - 1)) - col0;
+                    if (cl >= 0 && cl < BC) {
+                        C g = G[(size_t)cl * n0 + r];
+                        T q1 = ps[kW + t1];
+                        ar += q1 * g.x;
+                        ai += q1 * g.y;
+                    }
+                }
+                T q0 = ps[t0];
+                ar *= q0;
+                ai *= q0;
+            }
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            ar += __shfl_xor_sync(0xffffffffu, ar, o, 16);
+            ai += __shfl_xor_sync(0xffffffffu, ai, o, 16);
+        }
+        if (valid && t0 == 0) part[((size_t)b * smax + slot) * M + j] = mkc<T>(ar, ai);
+    }
+}
+
+// ================================================================ K3 combine + epilogue
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256)
+k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ nslots, int M,
+          int smax, int plane0, InterpArgs<T> a)
+{
+    using C = cplx_t<T>;
+    __shared__ double sh[32];
+    int b = blockIdx.y, gb = plane0 + b;
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double s0 = 0, s1 = 0;
+    if (j < M) {
+        int ns = nslots[j];
+        C f = part[((size_t)b * smax) * M + j];
+        for (int s = 1; s < ns; s++) {
+            C v = part[((size_t)b * smax + s) * M + j];
+            f.x += v.x;
+            f.y += v.y;
+        }
+        size_t o = (size_t)gb * a.out_stride + j;
+        if (MODE == IM_PLAIN) {
+            a.out[o] = f;
+        } else if (MODE == IM_RESID) {
+            C yv = a.y[(size_t)gb * a.y_stride + j];
+            a.out[o] = mkc<T>(yv.x - f.x, yv.y - f.y);
+        } else if (MODE == IM_DOTV) {
+            a.out[o] = f;
+            double wv = a.w ? (double)a.w[j] : 1.0;
+            s0 = wv * ((double)f.x * f.x + (double)f.y * f.y);
+        } else {
+            if (a.known[j / a.line_len]) {
+                C sv = a.s[(size_t)gb * a.s_stride + j];
+                a.out[o] = sv;
+                T dr = f.x - sv.x, di = f.y - sv.y, pr = f.x + sv.x, pi = f.y + sv.y;
+                s0 = (double)dr * dr + (double)di * di;
+                s1 = (double)pr * pr + (double)pi * pi;
+            } else {
+                a.out[o] = f;
+            }
+        }
+    }
+    if (MODE == IM_DOTV || MODE == IM_CONSTRAINT) {
+        double v0 = block_sum(s0, sh);
+        if (threadIdx.x == 0) a.part[(size_t)gb * a.part_stride + blockIdx.x] = v0;
+        if (MODE == IM_CONSTRAINT) {
+            double v1 = block_sum(s1, sh);
+            if (threadIdx.x == 0) a.part[(size_t)gb * a.part_stride + gridDim.x + blockIdx.x] = v1;
+        }
+    }
+}
+
+// ================================================================ K4 spread + column IFFT
+template <typename T, bool WEIGHTED>
+__global__ void __launch_bounds__(512)
+k_spread_colifft(SpreadArgs<T> sa, const int2 *__restrict__ u, const T *__restrict__ psi,
+                 const int *__restrict__ band_row, const int *__restrict__ band_off,
+                 const int *__restrict__ band_node, int W, int N0, int n0, int logn0, int n1,
+                 int BC, const cplx_t<T> *__restrict__ tw0, int plane0,
+                 cplx_t<T> *__restrict__ Hp)
+{
+    using C = cplx_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *S = (C *)smraw, *K = S + (size_t)BC * n0;  // sums and compensations (FFT scratch)
+    int cb = blockIdx.x, b = blockIdx.y, gb = plane0 + b;
+    for (int i = threadIdx.x; i < 2 * BC * n0; i += blockDim.x) S[i] = mkc<T>(0, 0);
+    __syncthreads();
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const C *f = sa.f + (size_t)gb * sa.f_stride;
+    int col0 = cb * BC;
+    for (int w = warp; w < W; w += blockDim.x >> 5) {
+        int rlo = band_row[cb * (W + 1) + w], rhi = band_row[cb * (W + 1) + w + 1];
+        int beg = band_off[cb * W + w], end = band_off[cb * W + w + 1];
+        for (int e = beg; e < end; e++) {
+            int j = band_node[e];
+            int2 uu = u[j];
+            C fv = f[j];
+            if (WEIGHTED) {
+                T wv = sa.w[j];
+                fv = mkc<T>(wv * fv.x, wv * fv.y);
+            }
+            T my = lane < 2 * kW ? psi[(size_t)j * 2 * kW + lane] : T(0);
+            for (int q = lane; q < kW * kW + 31; q += 32) {
+                int t0 = q / kW, t1 = q - t0 * kW;
+                T q0 = __shfl_sync(0xffffffffu, my, t0 < kW ? t0 : 0);
+                T q1 = __shfl_sync(0xffffffffu, my, kW + t1);
+                if (q < kW * kW) {
+                    int r = (uu.x + t0) & (n0 - 1);
+                    int cl = ((uu.y + t1) & (n1 - 1)) - col0;
+                    if (r >= rlo && r < rhi && cl >= 0 && cl < BC) {
+                        T vr = q1 * (q0 * fv.x), vi = q1 * (q0 * fv.y);
+                        size_t o = (size_t)cl * n0 + r;
+                        C sv = S[o];
+                        if (sizeof(T) == 4) {
+                            // Neumaier-compensated accumulation
+                            C kv = K[o];
+                            T tr = sv.x + vr, ti = sv.y + vi;
+                            kv.x += fabs(sv.x) >= fabs(vr) ? (sv.x - tr) + vr : (vr - tr) + sv.x;
+                            kv.y += fabs(sv.y) >= fabs(vi) ? (sv.y - ti) + vi : (vi - ti) + sv.y;
+                            S[o] = mkc<T>(tr, ti);
+                            K[o] = kv;
+                        } else {
+                            S[o] = mkc<T>(sv.x + vr, sv.y + vi);
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    if (sizeof(T) == 4)
+        for (int i = threadIdx.x; i < BC * n0; i += blockDim.x) {
+            C sv = S[i], kv = K[i];
+            S[i] = mkc<T>(sv.x + kv.x, sv.y + kv.y);
+        }
+    __syncthreads();
+    C *G = block_fft<T, +1>(S, K, n0, logn0, BC, tw0);
+    C *Hb = Hp + (size_t)b * N0 * n1 + col0;
+    for (int idx = threadIdx.x; idx < N0 * BC; idx += blockDim.x) {
+        int a = idx / BC, c = idx - a * BC;
+        int l0 = (a - N0 / 2) & (n0 - 1);
+        Hb[(size_t)a * n1 + c] = G[(size_t)c * n0 + l0];
+    }
+}
+
+// ================================================================ K5 row IFFT + crop
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256)
+k_rowifft_crop(const cplx_t<T> *__restrict__ Hp, int N0, int N1, int n1, int logn1, int kRows,
+               const T *__restrict__ c0, const T *__restrict__ c1,
+               const cplx_t<T> *__restrict__ tw1, int plane0, CropArgs<T> ca)
+{
+    using C = cplx_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double sh[32];
+    C *A = (C *)smraw, *B = A + kRows * n1;
+    int b = blockIdx.y, gb = plane0 + b, a0 = blockIdx.x * kRows;
+    int nr = min(kRows, N0 - a0);
+    const C *Hb = Hp + ((size_t)b * N0 + a0) * n1;
+    for (int idx = threadIdx.x; idx < nr * n1; idx += blockDim.x) A[idx] = Hb[idx];
+    __syncthreads();
+    C *R = block_fft<T, +1>(A, B, n1, logn1, nr, tw1);
+    double s = 0;
+    for (int idx = threadIdx.x; idx < nr * N1; idx += blockDim.x) {
+        int r = idx / N1, c = idx - r * N1;
+        int a = a0 + r;
+        int l1 = (c - N1 / 2) & (n1 - 1);
+        C g = R[r * n1 + l1];
+        T sc = c0[a] * c1[c];
+        C z = mkc<T>(g.x * sc, g.y * sc);
+        size_t o = (size_t)gb * ca.out_stride + (size_t)a * N1 + c;
+        ca.out[o] = z;
+        if (MODE == CM_INIT) ca.p_out[o] = z;
+        s += (double)z.x * z.x + (double)z.y * z.y;
+    }
+    if (MODE != CM_PLAIN) {
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) ca.part[(size_t)gb * ca.part_stride + blockIdx.x] = s;
+    }
+}
+
+// ================================================================ host side
+static int ilog2(int n)
+{
+    int l = 0;
+    while ((1 << l) < n) l++;
+    return l;
+}
+
+template <typename T> int NfftDev<T>::init_fused(const NfftTables &t)
+{
+    // column-block width: two BC x n0 complex buffers within 128 KB
+    int bc = (int)((128 << 10) / (2 * sizeof(C) * (size_t)t.n0));
+    if (bc > 32) bc = 32;
+    if (bc > t.n1) bc = t.n1;
+    int p = 1;
+    while (p * 2 <= bc) p *= 2;
+    bc = p;
+    if (bc < 1) return NUDIM_EINVAL;
+    FusedLists L;
+    if (build_fused_lists(t, bc, kFusedWarps, &L) != 0) {
+        set_error("fused NFFT list construction failed");
+        return NUDIM_EINVAL;
+    }
+    BC = L.BC;
+    nblk = L.nblk;
+    smax = L.smax;
+    // rows per CTA in the row passes: two rows x n1 complex buffers within 112 KB
+    rows = (int)((112 << 10) / (2 * sizeof(C) * (size_t)t.n1));
+    if (rows > 4) rows = 4;
+    std::vector<double> w0, w1;
+    fft_twiddles(n0, &w0);
+    fft_twiddles(n1, &w1);
+    std::vector<T> t0(w0.begin(), w0.end()), t1(w1.begin(), w1.end());
+    auto up = [&](void **dst, const void *srcp, size_t nb) -> int {
+        NUDIM_CUDA(cudaMalloc(dst, nb ? nb : 8));
+        if (nb) NUDIM_CUDA(cudaMemcpy(*dst, srcp, nb, cudaMemcpyHostToDevice));
+        bytes += nb;
+        return NUDIM_OK;
+    };
+    NUDIM_TRY(up((void **)&tw0, t0.data(), sizeof(T) * t0.size()));
+    NUDIM_TRY(up((void **)&tw1, t1.data(), sizeof(T) * t1.size()));
+    NUDIM_TRY(up((void **)&blk_off, L.blk_off.data(), sizeof(int) * L.blk_off.size()));
+    NUDIM_TRY(up((void **)&ent, L.ent.data(), sizeof(int) * L.ent.size()));
+    NUDIM_TRY(up((void **)&nslots, L.nslots.data(), L.nslots.size()));
+    NUDIM_TRY(up((void **)&band_row, L.band_row.data(), sizeof(int) * L.band_row.size()));
+    NUDIM_TRY(up((void **)&band_off, L.band_off.data(), sizeof(int) * L.band_off.size()));
+    NUDIM_TRY(up((void **)&band_node, L.band_node.data(), sizeof(int) * L.band_node.size()));
+    NUDIM_CUDA(cudaDeviceSynchronize());
+    size_t smem_col = 2 * sizeof(C) * (size_t)BC * n0;
+    size_t smem_row = 2 * sizeof(C) * (size_t)rows * n1;
+    if (smem_col > (227u << 10) || smem_row > (227u << 10) || rows < 1) {
+        set_error("fused NFFT: shared memory plan too large");
+        return NUDIM_EINVAL;
+    }
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft<T, PM_COMPLEX>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft<T, PM_REAL_INIT>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop<T, CM_PLAIN>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop<T, CM_DOT>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop<T, CM_INIT>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+    fused = true;
+    return NUDIM_OK;
+}
+
+template <typename T> void NfftDev<T>::release_fused()
+{
+    cudaFree(tw0);
+    cudaFree(tw1);
+    cudaFree(blk_off);
+    cudaFree(ent);
+    cudaFree(nslots);
+    cudaFree(band_row);
+    cudaFree(band_off);
+    cudaFree(band_node);
+    tw0 = tw1 = nullptr;
+    blk_off = ent = band_row = band_off = band_node = nullptr;
+    nslots = nullptr;
+    fused = false;
+}
+
+template <typename T> int NfftDev<T>::fused_chunk(int nplanes) const
+{
+    size_t per = sizeof(C) * ((size_t)N0 * n1 + (size_t)smax * M);
+    size_t budget = ctx->fused_budget ? ctx->fused_budget : ((size_t)96 << 20);
+    long c = (long)(budget / per);
+    if (c < 1) c = 1;
+    if (c > nplanes) c = nplanes;
+    return (int)c;
+}
+
+// Algorithmic bytes per launch (profiler), c = complex size:
+//   row pass  nb*c*(N0*N1 + N0*n1)     coefficients in, row spectra out
+//   col pass  nb*c*(N0*n1 + smax*M)    row spectra in, partials out (+ tables)
+//   combine   nb*c*(smax*M + M)        partials in, node values out
+template <typename T>
+int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia,
+                            cudaStream_t st)
+{
+    int chunk = fused_chunk(nplanes);
+    void *wsv;
+    size_t nH = (size_t)N0 * n1 * chunk, nP = (size_t)smax * M * chunk;
+    NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (nH + nP), &wsv));
+    C *H = (C *)wsv, *P = H + nH;
+    int logn0 = ilog2(n0), logn1 = ilog2(n1);
+    size_t smem_col = 2 * sizeof(C) * (size_t)BC * n0;
+    size_t smem_row = 2 * sizeof(C) * (size_t)rows * n1;
+    const double c = sizeof(C), tab = (double)M * (8 + 2 * kW * sizeof(T));
+    for (int p0 = 0; p0 < nplanes; p0 += chunk) {
+        int nb = std::min(chunk, nplanes - p0);
+        {
+            ProfScope ps(ctx, PK_PAD, st, nb * c * ((double)N0 * N1 + (double)N0 * n1));
+            dim3 g(ceil_div(N0, rows), nb);
+            if (pa.mode == PM_COMPLEX)
+                k_rowfft<T, PM_COMPLEX><<<g, 256, smem_row, st>>>(pa.src, pa.src_stride, N0, N1,
+                                                                   n1, logn1, rows, c0, c1, tw1,
+                                                                   p0, H, nullptr, 0);
+            else
+                k_rowfft<T, PM_REAL_INIT><<<g, 256, smem_row, st>>>(pa.src, pa.src_stride, N0,
+                                                                     N1, n1, logn1, rows, c0, c1,
+                                                                     tw1, p0, H, pa.f_init,
+                                                                     pa.f_stride);
+            NUDIM_LAUNCH_CHECK();
+        }
+        {
+            ProfScope ps(ctx, PK_INTERP, st,
+                         tab + nb * c * ((double)N0 * n1 + (double)smax * M));
+            k_colfft_interp<T><<<dim3(nblk, nb), 512, smem_col, st>>>(
+                H, N0, n0, logn0, n1, BC, tw0, u, psi, blk_off, ent, M, smax, P);
+            NUDIM_LAUNCH_CHECK();
+        }
+        {
+            ProfScope ps(ctx, PK_CGVEC, st, nb * c * ((double)smax * M + M));
+            dim3 g(interp_blocks(), nb);
+            switch (ia.mode) {
+            case IM_PLAIN: k_combine<T, IM_PLAIN><<<g, 256, 0, st>>>(P, nslots, M, smax, p0, ia); break;
+            case IM_RESID: k_combine<T, IM_RESID><<<g, 256, 0, st>>>(P, nslots, M, smax, p0, ia); break;
+            case IM_DOTV: k_combine<T, IM_DOTV><<<g, 256, 0, st>>>(P, nslots, M, smax, p0, ia); break;
+            default: k_combine<T, IM_CONSTRAINT><<<g, 256, 0, st>>>(P, nslots, M, smax, p0, ia); break;
+            }
+            NUDIM_LAUNCH_CHECK();
+        }
+    }
+    return NUDIM_OK;
+}
+
+//   spread    tables + nb*c*(M + N0*n1)   node values in, column spectra out
+//   row pass  nb*c*(N0*n1 + 2*N0*N1)      column spectra in, coefficients out
+template <typename T>
+int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca,
+                              cudaStream_t st)
+{
+    int chunk = fused_chunk(nplanes);
+    void *wsv;
+    size_t nH = (size_t)N0 * n1 * chunk;
+    NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (nH + (size_t)smax * M * chunk), &wsv));
+    C *Hp = (C *)wsv;
+    int logn0 = ilog2(n0), logn1 = ilog2(n1);
+    size_t smem_col = 2 * sizeof(C) * (size_t)BC * n0;
+    size_t smem_row = 2 * sizeof(C) * (size_t)rows * n1;
+    const double c = sizeof(C), tab = (double)M * (8 + 2 * kW * sizeof(T));
+    for (int p0 = 0; p0 < nplanes; p0 += chunk) {
+        int nb = std::min(chunk, nplanes - p0);
+        {
+            ProfScope ps(ctx, PK_SPREAD, st, tab + nb * c * ((double)M + (double)N0 * n1));
+            dim3 g(nblk, nb);
+            if (sa.w)
+                k_spread_colifft<T, true><<<g, 32 * kFusedWarps, smem_col, st>>>(
+                    sa, u, psi, band_row, band_off, band_node, kFusedWarps, N0, n0, logn0, n1, BC,
+                    tw0, p0, Hp);
+            else
+                k_spread_colifft<T, false><<<g, 32 * kFusedWarps, smem_col, st>>>(
+                    sa, u, psi, band_row, band_off, band_node, kFusedWarps, N0, n0, logn0, n1, BC,
+                    tw0, p0, Hp);
+            NUDIM_LAUNCH_CHECK();
+        }
+        {
+            ProfScope ps(ctx, PK_CROP, st, nb * c * ((double)N0 * n1 + 2.0 * N0 * N1));
+            dim3 g(ceil_div(N0, rows), nb);
+            switch (ca.mode) {
+            case CM_PLAIN: k_rowifft_crop<T, CM_PLAIN><<<g, 256, smem_row, st>>>(Hp, N0, N1, n1, logn1, rows, c0, c1, tw1, p0, ca); break;
+            case CM_DOT: k_rowifft_crop<T, CM_DOT><<<g, 256, smem_row, st>>>(Hp, N0, N1, n1, logn1, rows, c0, c1, tw1, p0, ca); break;
+            default: k_rowifft_crop<T, CM_INIT><<<g, 256, smem_row, st>>>(Hp, N0, N1, n1, logn1, rows, c0, c1, tw1, p0, ca); break;
+            }
+            NUDIM_LAUNCH_CHECK();
+        }
+    }
+    return NUDIM_OK;
+}
+
+template int NfftDev<double>::init_fused(const NfftTables &);
+template int NfftDev<float>::init_fused(const NfftTables &);
+template void NfftDev<double>::release_fused();
+template void NfftDev<float>::release_fused();
+template int NfftDev<double>::fused_chunk(int) const;
+template int NfftDev<float>::fused_chunk(int) const;
+template int NfftDev<double>::trafo_fused(int, const PadArgs<double> &, const InterpArgs<double> &,
+                                          cudaStream_t);
+template int NfftDev<float>::trafo_fused(int, const PadArgs<float> &, const InterpArgs<float> &,
+                                         cudaStream_t);
+template int NfftDev<double>::adjoint_fused(int, const SpreadArgs<double> &,
+                                            const CropArgs<double> &, cudaStream_t);
+template int NfftDev<float>::adjoint_fused(int, const SpreadArgs<float> &,
+                                           const CropArgs<float> &, cudaStream_t);
+
+}  // namespace nudim

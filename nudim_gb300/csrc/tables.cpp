@@ -217,3 +217,102 @@ void mt19937_uniform(uint32_t seed, size_t n, double *out)
 }
 
 }  // namespace nudim
+
+namespace nudim {
+
+void fft_twiddles(int n, std::vector<double> *tw)
+{
+    tw->resize(2 * (size_t)n);
+    for (int k = 0; k < n; k++) {
+        double a = 2.0 * kTruePi * (double)k / (double)n;
+        (*tw)[2 * k] = cos(a);
+        (*tw)[2 * k + 1] = -sin(a);
+    }
+}
+
+int build_fused_lists(const NfftTables &t, int BC, int W, FusedLists *L)
+{
+    const int kWin = 2 * 6 + 2;
+    if (BC <= 0 || t.n1 % BC || W <= 0) return -1;
+    int n0 = t.n0, n1 = t.n1, M = t.M;
+    L->BC = BC;
+    L->W = W;
+    L->nblk = n1 / BC;
+    int nblk = L->nblk;
+    // ---- trafo lists: blocks met by each node's 14 window columns
+    std::vector<std::vector<int>> per(nblk);
+    L->nslots.assign(M, 0);
+    L->smax = 0;
+    for (int j = 0; j < M; j++) {
+        int first = -1, slot = 0, last = -1;
+        for (int s = 0; s < kWin; s++) {
+            int b = ((t.u1[j] + s) & (n1 - 1)) / BC;
+            if (b == last) continue;
+            if (first < 0) first = b;
+            per[b].push_back(j * 8 + slot);
+            slot++;
+            last = b;
+        }
+        L->nslots[j] = (unsigned char)slot;
+        if (slot > L->smax) L->smax = slot;
+    }
+    if (L->smax > 8) return -1;
+    L->blk_off.assign(nblk + 1, 0);
+    for (int b = 0; b < nblk; b++) L->blk_off[b + 1] = L->blk_off[b] + (int)per[b].size();
+    L->ent.clear();
+    L->ent.reserve(L->blk_off[nblk]);
+    for (int b = 0; b < nblk; b++) L->ent.insert(L->ent.end(), per[b].begin(), per[b].end());
+    // ---- adjoint lists: per block, W bands of rows with balanced work
+    L->band_row.assign((size_t)nblk * (W + 1), 0);
+    L->band_off.assign((size_t)nblk * W + 1, 0);
+    L->band_node.clear();
+    std::vector<double> load(n0);
+    std::vector<std::vector<int>> bandlist(W);
+    for (int b = 0; b < nblk; b++) {
+        std::fill(load.begin(), load.end(), 0.0);
+        for (int e = L->blk_off[b]; e < L->blk_off[b + 1]; e++) {
+            int j = L->ent[e] / 8;
+            int cols = 0;
+            for (int s = 0; s < kWin; s++) cols += (((t.u1[j] + s) & (n1 - 1)) / BC) == b;
+            for (int s = 0; s < kWin; s++) load[(t.u0[j] + s) & (n0 - 1)] += cols + 2.0;
+        }
+        double tot = 0;
+        for (int r = 0; r < n0; r++) tot += load[r] + 1e-3;
+        int *br = &L->band_row[(size_t)b * (W + 1)];
+        br[0] = 0;
+        double acc = 0;
+        int w = 1;
+        for (int r = 0; r < n0 && w < W; r++) {
+            acc += load[r] + 1e-3;
+            while (w < W && acc >= tot * w / W) br[w++] = r + 1;
+        }
+        while (w < W) br[w++] = n0;
+        br[W] = n0;
+        for (int v = 0; v < W; v++) bandlist[v].clear();
+        for (int e = L->blk_off[b]; e < L->blk_off[b + 1]; e++) {
+            int j = L->ent[e] / 8;
+            int lastv = -1;
+            // window rows are 14 consecutive rows modulo n0; bands are
+            // contiguous row ranges, so collect each band once
+            bool hit[64] = {false};
+            for (int s = 0; s < kWin; s++) {
+                int r = (t.u0[j] + s) & (n0 - 1);
+                int v = 0;
+                while (v + 1 < W && r >= br[v + 1]) v++;
+                if (v != lastv && !hit[v]) {
+                    bandlist[v].push_back(j);
+                    hit[v] = true;
+                }
+                lastv = v;
+            }
+        }
+        for (int v = 0; v < W; v++) {
+            std::sort(bandlist[v].begin(), bandlist[v].end());
+            L->band_node.insert(L->band_node.end(), bandlist[v].begin(), bandlist[v].end());
+            L->band_off[(size_t)b * W + v + 1] = (int)L->band_node.size();
+        }
+    }
+    return 0;
+}
+
+}  // namespace nudim

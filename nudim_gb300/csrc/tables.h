@@ -35,6 +35,25 @@ struct NfftTables {
 
 int build_nfft_tables(int N0, int N1, int M, const double *x, int ty, int tx, NfftTables *t);
 
+// Work lists of the fused NFFT (column blocks of BC columns of the n0 x n1
+// oversampled grid):
+//   trafo:   per block, the nodes whose window columns meet the block, each
+//            with its partial slot (0 = the node's first block, 1, ...);
+//   adjoint: per block, W row bands balanced by window-cell count, and per
+//            (block, band) the nodes whose window meets that band.
+struct FusedLists {
+    int BC = 0, nblk = 0, W = 0, smax = 0;
+    std::vector<int> blk_off, ent;          // ent = node * 8 + slot
+    std::vector<unsigned char> nslots;      // blocks per node
+    std::vector<int> band_row;              // nblk * (W + 1) row boundaries
+    std::vector<int> band_off, band_node;   // CSR over (block, band)
+};
+
+int build_fused_lists(const NfftTables &t, int BC, int W, FusedLists *L);
+
+// e^{-2 pi i k / n}, k < n, interleaved (re, im)
+void fft_twiddles(int n, std::vector<double> *tw);
+
 // reconstruction.c:415-426 (--weight)
 void cgnr_weights(int A, int np, double padangle, double *w);
 

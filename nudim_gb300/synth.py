@@ -85,10 +85,11 @@ CONFIGS = {
 }
 
 
-def make_inputs(ctx, name, seed=MASTER_SEED):
-    """Phantom -> noisy tilt series for configuration `name` (GPU simulator)."""
+def make_inputs(ctx, name, seed=MASTER_SEED, cfg=None):
+    """Phantom -> noisy tilt series for configuration `name` (or the explicit
+    configuration dict `cfg`), simulated on the GPU."""
     from . import project_2d1d
-    c = CONFIGS[name]
+    c = cfg if cfg is not None else CONFIGS[name]
     vol = blob_phantom(seed=seed, **c["phantom"])
     s = c["sim"]
     proj = project_2d1d(ctx, vol, s["np"], s["gam_min"], s["gam_max"], s["interval"])

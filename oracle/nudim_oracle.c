@@ -505,11 +505,36 @@ void orc_ndft_adjoint(int N0, int N1, int M, const double *x, const double *f_d,
 typedef struct {
     cplx *r, *v, *z, *p, *wr;
     nfft_ws nw;
+    double noise;   /* test hook: relative noise on every NFFT output (0: off) */
+    uint64_t rng;
 } cg_ws;
+
+/* splitmix64 + Box-Muller: Gaussian noise for the perturbation hook */
+static double gauss(uint64_t *s)
+{
+    uint64_t z[2];
+    for (int q = 0; q < 2; q++) {
+        uint64_t x = (*s += 0x9e3779b97f4a7c15ull);
+        x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+        x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+        z[q] = x ^ (x >> 31);
+    }
+    double u1 = ((double)(z[0] >> 11) + 1.0) / 9007199254740993.0;
+    double u2 = (double)(z[1] >> 11) / 9007199254740992.0;
+    return sqrt(-2.0 * log(u1)) * cos(2.0 * TRUE_PI * u2);
+}
+
+static void perturb(cg_ws *c, cplx *v, size_t n)
+{
+    if (!c->noise) return;
+    for (size_t i = 0; i < n; i++) v[i] *= 1.0 + c->noise * gauss(&c->rng);
+}
 
 static void cg_init(cg_ws *c, const orc_nfft *p)
 {
     size_t M = (size_t)p->M, N = (size_t)p->N0 * p->N1;
+    c->noise = 0;
+    c->rng = 0;
     c->r = (cplx *)malloc(sizeof(cplx) * M);
     c->v = (cplx *)malloc(sizeof(cplx) * M);
     c->wr = (cplx *)malloc(sizeof(cplx) * M);
@@ -538,11 +563,13 @@ static void cgnr_ws(const orc_nfft *pl, cg_ws *c, const cplx *y, const double *w
 {
     int M = pl->M, N = pl->N0 * pl->N1;
     nfft_trafo_ws(pl, &c->nw, f, c->v);
+    perturb(c, c->v, M);
     for (int j = 0; j < M; j++) {
         c->r[j] = y[j] - c->v[j];
         c->wr[j] = w ? w[j] * c->r[j] : c->r[j];
     }
     nfft_adjoint_ws(pl, &c->nw, c->wr, c->z);
+    perturb(c, c->z, N);
     double dot_z = 0;
     for (int k = 0; k < N; k++) {
         dot_z += cabs2(c->z[k]);
@@ -551,6 +578,7 @@ static void cgnr_ws(const orc_nfft *pl, cg_ws *c, const cplx *y, const double *w
     if (trace) trace[0] = dot_z;
     for (int it = 0; it < iters; it++) {
         nfft_trafo_ws(pl, &c->nw, c->p, c->v);
+        perturb(c, c->v, M);
         double dot_v = 0;
         for (int j = 0; j < M; j++) dot_v += (w ? w[j] : 1.0) * cabs2(c->v[j]);
         double alpha = dot_z / dot_v;
@@ -560,6 +588,7 @@ static void cgnr_ws(const orc_nfft *pl, cg_ws *c, const cplx *y, const double *w
             c->wr[j] = w ? w[j] * c->r[j] : c->r[j];
         }
         nfft_adjoint_ws(pl, &c->nw, c->wr, c->z);
+        perturb(c, c->z, N);
         double dot_z_new = 0;
         for (int k = 0; k < N; k++) dot_z_new += cabs2(c->z[k]);
         double beta = dot_z_new / dot_z;
@@ -575,6 +604,20 @@ void orc_cgnr(orc_nfft *p, const double *y, const double *w, double *f_hat_iter,
     cg_ws c;
     cg_init(&c, p);
     cgnr_ws(p, &c, (const cplx *)y, w, (cplx *)f_hat_iter, iters, trace);
+    cg_free(&c);
+}
+
+/* Test hook: CGNR with every NFFT output multiplied by (1 + eps N(0,1)).
+ * Measures how far the solver itself moves under operator errors of a
+ * given size (the floor against which a reduced-precision solver is held). */
+void orc_cgnr_perturbed(orc_nfft *p, const double *y, const double *w, double *f_hat_iter,
+                        int iters, double eps, unsigned long seed)
+{
+    cg_ws c;
+    cg_init(&c, p);
+    c.noise = eps;
+    c.rng = seed;
+    cgnr_ws(p, &c, (const cplx *)y, w, (cplx *)f_hat_iter, iters, NULL);
     cg_free(&c);
 }
 

@@ -57,6 +57,9 @@ void orc_ndft_adjoint(int N0, int N1, int M, const double *x, const double *f,
 /* ---- CGNR (solver_before_loop_complex + iters x solver_loop_one_step) ---- */
 void orc_cgnr(orc_nfft *p, const double *y, const double *w, double *f_hat_iter,
               int iters, double *dot_z_trace);
+/* Same with every NFFT output multiplied by (1 + eps N(0,1)) (test floor). */
+void orc_cgnr_perturbed(orc_nfft *p, const double *y, const double *w, double *f_hat_iter,
+                        int iters, double eps, unsigned long seed);
 
 /* ---- FFT (fftw_plan_many_dft semantics, unnormalised) ---- */
 void orc_fft_many(double *data, int n, int howmany, int stride, int dist, int sign);

@@ -64,6 +64,8 @@ def lib():
         L.orc_ndft_trafo.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
         L.orc_ndft_adjoint.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
         L.orc_cgnr.argtypes = [C.c_void_p, _dp, C.c_void_p, _dp, C.c_int, C.c_void_p]
+        L.orc_cgnr_perturbed.argtypes = [C.c_void_p, _dp, C.c_void_p, _dp, C.c_int, C.c_double,
+                                         C.c_ulong]
         L.orc_fft_many.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_tv_discrete.argtypes = [_dp, _dp, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_tv_discrete_height.argtypes = [_dp, _dp, C.c_float, C.c_int, C.c_int, C.c_int,
@@ -166,6 +168,14 @@ class NFFT:
                        f.view(np.float64), iters, None if tr is None else tr.ctypes.data)
         f = f.reshape(self.N0, self.N1)
         return (f, tr) if trace else f
+
+    def cgnr_perturbed(self, y, f0, eps, w=None, iters=10, seed=1):
+        """CGNR with every NFFT output multiplied by (1 + eps N(0,1))."""
+        f = np.array(f0, dtype=np.complex128).reshape(-1).copy()
+        wv = None if w is None else _c(w)
+        lib().orc_cgnr_perturbed(self._p, _cplx_view(y), None if wv is None else wv.ctypes.data,
+                                 f.view(np.float64), iters, eps, seed)
+        return f.reshape(self.N0, self.N1)
 
 
 def ndft_trafo(N0, N1, x, f_hat):

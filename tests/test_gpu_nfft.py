@@ -96,11 +96,47 @@ def test_cgnr_vs_oracle(gpu_ctx, orc, nudim_built, weighted, prec):
     f = f_d.cpu().numpy()
     for b in range(B):
         fo = ref.cgnr(y[b], f0[b], w=w, iters=10)
-        if prec == 0:
-            assert rel(f[b], fo) < 1e-9
-        else:
-            # FP32: within 10x of the oracle's own change under a 1e-7
-            # (single-precision sized) perturbation of the data
-            yp = y[b] * (1 + 1e-7 * np.random.default_rng(b).standard_normal(M))
-            floor = rel(ref.cgnr(yp, f0[b], w=w, iters=10), fo)
-            assert rel(f[b], fo) < max(1e-5, 10 * floor)
+        # Bar: 10x the oracle's own change when every one of its NFFT outputs
+        # carries relative noise of the size the form's rounding leaves
+        # (1e-13 FP64, 1e-6 FP32), and at least 1e-9 (FP64) / 1e-5 (FP32).
+        # Unweighted CGNR on the polar set amplifies such operator noise
+        # ~1e6-fold in 10 steps; with the density weights it does not.
+        eps, lo = (1e-13, 1e-9) if prec == 0 else (1e-6, 1e-5)
+        floor = rel(ref.cgnr_perturbed(y[b], f0[b], eps, w=w, iters=10, seed=b + 1), fo)
+        assert rel(f[b], fo) < max(lo, 10 * floor)
+
+
+@pytest.mark.parametrize("N0,N1,kind,prec", [(32, 32, "polar", 0), (48, 40, "random", 0),
+                                             (128, 128, "polar", 0), (384, 384, "polar", 1),
+                                             (20, 12, "uniform", 1), (64, 64, "polar", 1)])
+def test_fused_path_matches_grid_path(nudim_built, orc, N0, N1, kind, prec):
+    """The default fused NFFT (grid kept on chip) against the cuFFT grid path
+    and the oracle on the same inputs."""
+    import torch
+    ctx_f = nudim_built.Context(0)
+    ctx_g = nudim_built.Context(0, nudim_built.CTX_GRID_NFFT)
+    x = nodes(orc, N0, N1, kind, N0) if N0 != 384 else orc.polar_nodes(-60, 60, 2, 1, 384)
+    M, B = len(x), 2
+    rng = np.random.default_rng(N0 * 3 + N1)
+    fh = rng.standard_normal((B, N0, N1)) + 1j * rng.standard_normal((B, N0, N1))
+    y = rng.standard_normal((B, M)) + 1j * rng.standard_normal((B, M))
+    outs = []
+    for ctx in (ctx_f, ctx_g):
+        plan = nudim_built.NfftPlan(ctx, N0, N1, x, prec)
+        fh_d, y_d = to_dev(fh, cdtype(prec)), to_dev(y, cdtype(prec))
+        f_d = torch.zeros((B, M), dtype=fh_d.dtype, device="cuda")
+        g_d = torch.zeros((B, N0, N1), dtype=fh_d.dtype, device="cuda")
+        plan.trafo(B, fh_d.data_ptr(), f_d.data_ptr())
+        plan.adjoint(B, y_d.data_ptr(), g_d.data_ptr())
+        torch.cuda.synchronize()
+        outs.append((f_d.cpu().numpy(), g_d.cpu().numpy()))
+        plan.close()
+    ref = orc.NFFT(N0, N1, x)
+    tol = 1e-12 if prec == 0 else 2e-5
+    for b in range(B):
+        rf, rg = ref.trafo(fh[b]), ref.adjoint(y[b])
+        assert rel(outs[0][0][b], rf) < tol and rel(outs[0][1][b], rg) < tol
+        assert rel(outs[0][0][b], outs[1][0][b]) < tol
+        assert rel(outs[0][1][b], outs[1][1][b]) < tol
+    ctx_f.close()
+    ctx_g.close()
