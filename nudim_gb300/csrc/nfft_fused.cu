@@ -284,7 +284,10 @@ k_spread_colifft(SpreadArgs<T> sa, const int2 *__restrict__ u, const T *__restri
                 fv = mkc<T>(wv * fv.x, wv * fv.y);
             }
             T my = lane < 2 * kW ? psi[(size_t)j * 2 * kW + lane] : T(0);
-            for (int q = lane; q < kW * kW + 31; q += 32) {
+            // every lane runs the same number of iterations: the shuffles
+            // below need all 32 lanes each time
+            for (int qb = 0; qb < kW * kW; qb += 32) {
+                int q = qb + lane;
                 int t0 = q / kW, t1 = q - t0 * kW;
                 T q0 = __shfl_sync(0xffffffffu, my, t0 < kW ? t0 : 0);
                 T q1 = __shfl_sync(0xffffffffu, my, kW + t1);
