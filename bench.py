@@ -66,6 +66,11 @@ def barrier(dist):
         dist.barrier()
 
 
+def log(msg):
+    """Progress of the legs on stderr (stdout carries only the JSON line)."""
+    print("[bench] " + msg, file=sys.stderr, flush=True)
+
+
 def max_over_ranks(dist, v, device=None):
     """Largest value over ranks (the slowest rank's time)."""
     if dist is None:
@@ -164,21 +169,26 @@ def job_kwargs(r, precision):
                 variant=ng.VARIANT_SERIAL)
 
 
-def stream_events(ctx):
+def stream_events(job):
     import torch
-    st = torch.cuda.ExternalStream(ctx.stream)
+    st = torch.cuda.ExternalStream(job.stream)
     return st, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def timed_steps(ctx, job, steps):
-    """Device time (ms) of `steps` outer iterations on the context stream."""
+def timed_steps(ctx, job, steps, nvtx=None):
+    """Device time (ms) of `steps` outer iterations on the job's stream.
+    `nvtx` names a push/pop range around the launches (a filter for ncu)."""
     import torch
-    st, e0, e1 = stream_events(ctx)
+    st, e0, e1 = stream_events(job)
     torch.cuda.synchronize()
+    if nvtx:
+        torch.cuda.nvtx.range_push(nvtx)
     e0.record(st)
     for _ in range(steps):
         job.step(1)
     e1.record(st)
+    if nvtx:
+        torch.cuda.nvtx.range_pop()
     e1.synchronize()
     torch.cuda.synchronize()
     return e0.elapsed_time(e1)
@@ -226,6 +236,65 @@ def cpu_baseline_sample(proj, r, iters=1, threads=None):
                       "Z-planes (one per thread) extrapolated linearly, volume phases on the "
                       "full volume; setup %.1f s untimed" % (iters, nplanes, r["nz"], t_setup),
             "s_per_iter": t_iter}
+
+
+def serving_specs(n_jobs, seed):
+    """Uneven jobs of the batched/serving configurations: nx from
+    {96,128,160,192,256}, nz from 32..256 step 16, pad = round16(U(1.25,1.5)
+    * nx), symmetric max tilt U{45..70}, step {1,2,3}; one job in ten is
+    384 x 384 x 192 (pad 480..576).  20 HIO + 30 ER, TV, --weight."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_jobs):
+        if rng.uniform() < 0.1:
+            nx, nz = 384, 192
+        else:
+            nx = int(rng.choice([96, 128, 160, 192, 256]))
+            nz = int(rng.integers(2, 17)) * 16
+        npad = int(round(rng.uniform(1.25, 1.5) * nx / 16.0)) * 16
+        step = int(rng.choice([1, 2, 3]))
+        gmax = int(rng.integers(45, 71))
+        gmax -= gmax % step
+        out.append(dict(nx=nx, nz=nz, np=npad, gam_min=-gmax, gam_max=gmax, interval=step,
+                        padangle=1, nhio=10, ner=10, denoise=1, weight=1, seed=seed + k))
+    return out
+
+
+def serving_bench(ctx, n_jobs, rate, precision, seed=20261205):
+    """Poisson arrivals at `rate` jobs/s into the continuous-batching server;
+    returns p50/p99 arrival-to-result latency and completed jobs/s."""
+    import torch
+
+    import nudim_gb300 as ng
+    from nudim_gb300.synth import add_noise, blob_phantom
+    specs = serving_specs(n_jobs, seed)
+    inputs = []
+    for sp in specs:
+        s = dict(sp)
+        sd = s.pop("seed")
+        nx, nz = s["nx"], s["nz"]
+        vol = blob_phantom((nz, nx, nx), nblobs=30, radius=0.35 * nx, sigma_range=(2, 8),
+                           amp_range=(0.2, 1.0), seed=sd)
+        proj = ng.project_2d1d(ctx, vol, nx, s["gam_min"], s["gam_max"], s["interval"])
+        inputs.append((add_noise(proj, 1.0, sd + 1), s))
+    arrivals = np.cumsum(np.random.default_rng(seed + 7).exponential(1.0 / rate, n_jobs))
+    free, _ = torch.cuda.mem_get_info()
+    srv = ng.Server(ctx, int(0.7 * free), max_active=16)
+    t0 = time.perf_counter()
+    tickets = []
+    for (proj, s), ta in zip(inputs, arrivals):
+        dt = t0 + ta - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        tickets.append(srv.submit(proj, precision=precision, **s))
+    for t in tickets:
+        srv.wait(t, volume=False)
+    st = srv.stats()
+    srv.close()
+    log("serving: %d jobs, p50 %.3f s, p99 %.3f s" % (n_jobs, st.get("p50_s", -1), st.get("p99_s", -1)))
+    st.update(arrival_rate_jobs_per_s=rate, jobs=n_jobs,
+              voxels_per_job_mean=float(np.mean([s["nz"] * s["np"] ** 2 for _, s in inputs])))
+    return st
 
 
 # ------------------------------------------------------------------ arms
@@ -317,15 +386,25 @@ def run_ours(args):
     clocks = ClockSampler(local)
     clocks.start()
     n0 = ng.lib().nudim_launch_count()
-    ctx.profile(True)
-    ms = timed_steps(ctx, job, args.steps)
-    prof = ctx.profile_read()
-    ctx.profile(False)
+    ms = timed_steps(ctx, job, args.steps, "timed")  # graph replay of each iteration
     launches = int(ng.lib().nudim_launch_count() - n0)
     clk = clocks.stop()
     ms_max = max_over_ranks(dist, ms, dev)
     value = ws * V * args.steps / (ms_max / 1e3)
-    top, roof, shares = roofline_from_profile(prof, peaks.get("hbm_gbs", 6800.0), peak_kind)
+    log("mixed: %.2f ms/iteration, %.3e voxel-iters/s, %d launches" % (ms_max / args.steps, value, launches))
+    # per-kernel CUDA events on the job stream over further iterations of the
+    # same job (event timing runs the launches eagerly, without graph replay)
+    prof_steps = min(2, r["nhio"] + r["ner"] - args.warmup - args.steps)
+    if prof_steps > 0:
+        ctx.profile(True)
+        ms_prof = timed_steps(ctx, job, prof_steps, "profiled")
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        top, roof, shares = roofline_from_profile(prof, peaks.get("hbm_gbs", 6800.0), peak_kind)
+        roof["profiled_ms_per_step"] = ms_prof / prof_steps
+        log("profiled pass: top kernel %s, %.1f%% of measured HBM" % (top, 100 * roof["frac"]))
+    else:
+        roof, shares = None, None
     job.close()
 
     # ---- e2e through the C ABI: host tilt series in, host volume out
@@ -345,6 +424,7 @@ def run_ours(args):
                "h2d_bytes_per_step": int(proj.nbytes // args.steps),
                "d2h_bytes_per_step": int(out.nbytes // args.steps),
                "includes": "job setup (tilt-series NFFT, slice reorder, initial inverse NFFT)"}
+        log("e2e: %.3e voxel-iters/s" % e2e["value"])
 
     # ---- FP64 plain form on the same job (fewer steps: it is the slow form)
     v64 = ms64 = err = None
@@ -360,6 +440,7 @@ def run_ours(args):
         ms64 = max_over_ranks(dist, ms64, dev)
         v64 = ws * V * fp64_steps / (ms64 / 1e3)
         err = float(np.linalg.norm(vol_mixed_w - vol64_w) / np.linalg.norm(vol64_w))
+        log("fp64: %.2f ms/iteration, mixed vs fp64 rel L2 %.2e" % (ms64 / fp64_steps, err))
 
     line = {
         "metric": "voxel-iters/s", "value": value, "unit": "voxel-iters/s", "n_gpus": ws,
@@ -377,6 +458,11 @@ def run_ours(args):
                               "ms_per_step": ms64 / fp64_steps, "steps": fp64_steps}
         line["mixed_over_fp64"] = value / v64
         line["rel_l2_mixed_vs_fp64_after_warmup"] = err
+    if args.serve_jobs > 0:
+        line["serving"] = {"mixed": serving_bench(ctx, args.serve_jobs, args.serve_rate, ng.MIXED)}
+        if args.serve_fp64:
+            line["serving"]["fp64_plain"] = serving_bench(ctx, args.serve_jobs, args.serve_rate,
+                                                          ng.FP64)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(proj, r)
     ctx.close()
@@ -398,6 +484,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--serve-jobs", type=int, default=16,
+                    help="jobs in the serving measurement (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=0.5, help="Poisson arrivals, jobs/s")
+    ap.add_argument("--serve-fp64", action="store_true", help="also serve the FP64 form")
     ap.add_argument("--nz", type=int, default=0,
                     help="override the number of Z-planes (small-case profiling only)")
     args = ap.parse_args()

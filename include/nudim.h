@@ -138,11 +138,17 @@ int nudim_job_set_projections(nudim_job *job, const double *proj, size_t n);
 
 /* Run `iters` outer HIO/ER iterations (reconstruction.c:545-703) of each
  * job; the iteration counter of each job continues from where it stopped
- * and never passes nhio+ner.  Jobs on one context run back to back on the
- * context stream; the call returns when the work is queued (sync with
- * nudim_ctx_sync or by reading results). */
+ * and never passes nhio+ner.  Iterations are queued round-robin over the
+ * jobs, each on its own stream, so they overlap on the device; the call
+ * returns when the work is queued (sync with nudim_job_sync, nudim_ctx_sync
+ * or by reading results). */
 int nudim_step(nudim_ctx *ctx, nudim_job *const *jobs, int njobs, int iters);
+/* Wait for all queued work of every job on the context's device. */
 int nudim_ctx_sync(nudim_ctx *ctx);
+/* Each job owns a CUDA stream (its allocations, transforms and kernels are
+ * ordered on it), so the jobs of one nudim_step call overlap on the device. */
+void *nudim_job_stream(nudim_job *job);
+int nudim_job_sync(nudim_job *job);
 
 /* Copy the current volume to host FP64.  crop=0: full nz*np*np volume
  * (recovered-0.txt layout); crop=1: central nx*nx crop of every plane in
@@ -158,6 +164,33 @@ int nudim_job_iterations_done(nudim_job *job, int *done);
  * (the reference's grad_before/grad_after dumps).  Host buffers of
  * nz*np*np doubles each stay owned by the caller; pass nn < 0 to disable. */
 int nudim_job_set_denoise_dump(nudim_job *job, int nn, double *before, double *after);
+
+/* ------------------------------------------------------------------ */
+/* serving: continuous batching of reconstruction jobs (no counterpart */
+/* in the reference, which reconstructs one tomogram per process)     */
+/* ------------------------------------------------------------------ */
+typedef struct nudim_server nudim_server;
+
+/* A request loop on its own host thread: queued requests are admitted while
+ * their device-memory footprint (nudim_job_footprint plus workspace) fits
+ * mem_budget and fewer than max_active jobs run; admitted jobs stay
+ * resident, their outer iterations are queued round-robin on per-job
+ * streams (at most two in flight each) so they overlap on the device, and a
+ * finished job's volume is copied out and its memory released. */
+int nudim_server_create(nudim_ctx *ctx, size_t mem_budget, int max_active, nudim_server **out);
+/* Thread-safe; copies the tilt series; the arrival time is stamped here. */
+int nudim_server_submit(nudim_server *s, const nudim_job_desc *desc, const double *proj,
+                        size_t n, long long *ticket);
+/* Block until the ticket's job is done; copy its volume (crop as in
+ * nudim_job_get_volume; vol may be NULL) and its arrival-to-result latency. */
+int nudim_server_wait(nudim_server *s, long long ticket, double *vol, size_t n, int crop,
+                      double *latency_s);
+/* Completed jobs, median and 99th-percentile latency (s), completed jobs per
+ * second from the first arrival to the last completion. */
+int nudim_server_stats(nudim_server *s, long long *completed, double *p50_s, double *p99_s,
+                       double *jobs_per_s);
+/* Finish every submitted job, then stop the loop. */
+int nudim_server_destroy(nudim_server *s);
 
 /* projection_sim -m 2D1D (src/projection_sim.c:282-405) on the GPU, FP64:
  * density [nz][ny][nx] (host) -> tilt series [tilt][nz][np] (host), tilts

@@ -32,6 +32,8 @@ EXPORTS = [
     ("nudim_profile_kernel_count", _ip, []),
     ("nudim_profile_kernel_name", C.c_char_p, [_ip]),
     ("nudim_launch_count", C.c_ulonglong, []),
+    ("nudim_job_stream", _vp, [_vp]),
+    ("nudim_job_sync", _ip, [_vp]),
     ("nudim_job_footprint", _ip, [_vp, C.POINTER(_sz)]),
     ("nudim_job_create", _ip, [_vp, _vp, C.POINTER(_vp)]),
     ("nudim_job_destroy", _ip, [_vp]),
@@ -43,6 +45,11 @@ EXPORTS = [
     ("nudim_job_get_rfactor", _ip, [_vp, _dp, _ip, C.POINTER(_ip)]),
     ("nudim_job_iterations_done", _ip, [_vp, C.POINTER(_ip)]),
     ("nudim_job_set_denoise_dump", _ip, [_vp, _ip, _dp, _dp]),
+    ("nudim_server_create", _ip, [_vp, _sz, _ip, C.POINTER(_vp)]),
+    ("nudim_server_submit", _ip, [_vp, _vp, _dp, _sz, C.POINTER(C.c_longlong)]),
+    ("nudim_server_wait", _ip, [_vp, C.c_longlong, _dp, _sz, _ip, _dp]),
+    ("nudim_server_stats", _ip, [_vp, C.POINTER(C.c_longlong), _dp, _dp, _dp]),
+    ("nudim_server_destroy", _ip, [_vp]),
     ("nudim_project_2d1d", _ip, [_vp, _dp, _ip, _ip, _ip, _ip, C.c_double, C.c_double,
                              C.c_double, C.c_double, C.c_ulong, _dp, _sz]),
     ("nudim_nfft_plan_create", _ip, [_vp, _ip, _ip, _ip, _dp, _ip, C.POINTER(_vp)]),
@@ -196,6 +203,14 @@ class Job:
     def step(self, iters):
         self.ctx.step([self], iters)
 
+    @property
+    def stream(self):
+        """The job's CUDA stream (cudaStream_t as an int)."""
+        return lib().nudim_job_stream(self.h)
+
+    def sync(self):
+        _check(lib().nudim_job_sync(self.h))
+
     def volume(self, crop=False):
         d = self.desc
         shp = (d.nz, d.nx, d.nx) if crop else self.shape
@@ -230,6 +245,54 @@ class Job:
     def close(self):
         if getattr(self, "h", None):
             lib().nudim_job_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request loop (nudim_server_*)."""
+
+    def __init__(self, ctx, mem_budget_bytes, max_active=16):
+        self.ctx = ctx
+        h = C.c_void_p()
+        _check(lib().nudim_server_create(ctx.h, int(mem_budget_bytes), max_active, C.byref(h)))
+        self.h = h
+        self.desc = {}
+
+    def submit(self, proj, **kw):
+        d = make_desc(**kw)
+        p = np.ascontiguousarray(proj, np.float64)
+        t = C.c_longlong()
+        _check(lib().nudim_server_submit(self.h, C.byref(d), _dptr(p), p.size, C.byref(t)))
+        self.desc[t.value] = d
+        return t.value
+
+    def wait(self, ticket, volume=True):
+        d = self.desc[ticket]
+        lat = C.c_double()
+        if volume:
+            out = np.zeros((d.nz, d.np, d.np))
+            _check(lib().nudim_server_wait(self.h, ticket, _dptr(out), out.size, 0,
+                                           C.byref(lat)))
+            return out, lat.value
+        _check(lib().nudim_server_wait(self.h, ticket, None, 0, 0, C.byref(lat)))
+        return None, lat.value
+
+    def stats(self):
+        n, p50, p99, tput = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
+        _check(lib().nudim_server_stats(self.h, C.byref(n), C.byref(p50), C.byref(p99),
+                                        C.byref(tput)))
+        return dict(completed=n.value, p50_s=p50.value, p99_s=p99.value,
+                    jobs_per_s=tput.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().nudim_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -94,12 +94,19 @@ template <typename T> struct JobState {
     int part_stride = 0, tv_cap = 0;
     size_t bytes = 0;
     std::vector<void *> owned;
+    cudaStream_t st = nullptr;  // the job's stream: every allocation is ordered on it
+    cufftHandle zplan = 0;      // Z-axis FFT plan with its work area in zws
+    Workspace zws;
+    int *it = nullptr;          // device copy of the outer-iteration index
+    cudaGraphExec_t gexec = nullptr;  // replay of one outer iteration
+    bool graph_tried = false;
+    unsigned long long graph_kernels = 0;
 
     template <typename P> int alloc(P **ptr, size_t n)
     {
         size_t b = sizeof(P) * (n ? n : 1);
         void *q = nullptr;
-        NUDIM_CUDA(cudaMalloc(&q, b));
+        NUDIM_CUDA(cudaMallocAsync(&q, b, st));
         owned.push_back(q);
         bytes += b;
         *ptr = (P *)q;
@@ -107,9 +114,15 @@ template <typename T> struct JobState {
     }
     void release()
     {
-        for (void *q : owned) cudaFree(q);
+        for (void *q : owned) cudaFreeAsync(q, st);
         owned.clear();
         pl.release();
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        graph_tried = false;
+        if (zplan) cufftDestroy(zplan);
+        zplan = 0;
+        ws_release(&zws);
         live = false;
     }
 };
@@ -120,6 +133,8 @@ using namespace nudim;
 
 struct nudim_job {
     nudim_ctx *ctx = nullptr;
+    cudaStream_t stream = nullptr;  // own stream: jobs overlap on the device
+    Workspace ws;                   // NFFT scratch of this job
     nudim_job_desc d{};
     int A = 0, M = 0, nmeas = 0, n_unk_row = 0;
     double pad_min = 0, pad_max = 0;
@@ -148,33 +163,34 @@ struct nudim_nfft_plan {
 namespace nudim {
 
 // ================================================================ Z-FFT
-static int zfft_plan(nudim_ctx *ctx, int nz, int P2, int prec, cufftHandle *h)
+// fftw_plan_many_dft(1, &nz, np*np, data, NULL, np*np, 1, ...)
+// (reconstruction.c:556): one plan per job state, its work area allocated
+// stream-ordered so that plan creation never synchronises the device.
+template <typename T> static int zfft_plan(nudim_job *jb, JobState<T> &s)
 {
-    auto key = std::make_tuple(nz, P2, prec, 0);
-    auto it = ctx->fftz.find(key);
-    if (it != ctx->fftz.end()) {
-        *h = it->second;
-        return NUDIM_OK;
-    }
+    if (s.zplan) return NUDIM_OK;
+    int P2 = jb->d.np * jb->d.np;
+    int n[1] = {jb->d.nz};
+    size_t work = 0;
     cufftHandle p;
-    int n[1] = {nz};
-    // fftw_plan_many_dft(1, &nz, np*np, data, NULL, np*np, 1, ...) (reconstruction.c:556)
-    NUDIM_CUFFT(cufftPlanMany(&p, 1, n, n, P2, 1, n, P2, 1,
-                              prec == NUDIM_FP64 ? CUFFT_Z2Z : CUFFT_C2C, P2));
-    ctx->fftz[key] = p;
-    *h = p;
+    NUDIM_CUFFT(cufftCreate(&p));
+    NUDIM_CUFFT(cufftSetAutoAllocation(p, 0));
+    NUDIM_CUFFT(cufftMakePlanMany(p, 1, n, n, P2, 1, n, P2, 1, fft_c2c<T>(), P2, &work));
+    void *wa = nullptr;
+    s.zws.st = s.st;
+    NUDIM_TRY(ws_get(&s.zws, work ? work : 256, &wa));
+    NUDIM_CUFFT(cufftSetWorkArea(p, wa));
+    NUDIM_CUFFT(cufftSetStream(p, s.st));
+    s.zplan = p;
     return NUDIM_OK;
 }
 
 template <typename T> static int zfft(nudim_job *jb, JobState<T> &s, int dir)
 {
-    cufftHandle h;
+    NUDIM_TRY(zfft_plan<T>(jb, s));
     int P2 = jb->d.np * jb->d.np;
-    NUDIM_TRY(zfft_plan(jb->ctx, jb->d.nz, P2, prec_of<T>(), &h));
-    NUDIM_CUFFT(cufftSetStream(h, jb->ctx->stream));
-    ProfScope ps(jb->ctx, PK_ZFFT, jb->ctx->stream,
-                 2.0 * sizeof(cplx_t<T>) * (double)P2 * jb->d.nz);
-    return fft_exec<T>(h, s.data, dir);
+    ProfScope ps(jb->ctx, PK_ZFFT, s.st, 2.0 * sizeof(cplx_t<T>) * (double)P2 * jb->d.nz);
+    return fft_exec<T>(s.zplan, s.data, dir);
 }
 
 // ================================================================ job state setup
@@ -183,7 +199,8 @@ template <typename T> static int state_init(nudim_job *jb, JobState<T> &s)
     if (s.live) return NUDIM_OK;
     int nz = jb->d.nz, np = jb->d.np, M = jb->M;
     size_t P2 = (size_t)np * np, V = P2 * nz;
-    NUDIM_TRY(s.pl.init(jb->ctx, jb->tabs));
+    s.st = jb->stream;
+    NUDIM_TRY(s.pl.init(jb->ctx, jb->tabs, jb->stream, &jb->ws));
     s.bytes += s.pl.bytes;
     NUDIM_TRY(s.alloc(&s.img_a, V));
     NUDIM_TRY(s.alloc(&s.img_b, V));
@@ -196,15 +213,14 @@ template <typename T> static int state_init(nudim_job *jb, JobState<T> &s)
     NUDIM_TRY(s.alloc(&s.slices, (size_t)nz * M));
     NUDIM_TRY(s.alloc(&s.known, jb->A));
     NUDIM_CUDA(cudaMemcpyAsync(s.known, jb->known.data(), sizeof(int) * jb->A,
-                               cudaMemcpyHostToDevice, jb->ctx->stream));
+                               cudaMemcpyHostToDevice, jb->stream));
     if (jb->d.weight) {
         std::vector<double> wd(M);
         cgnr_weights(jb->A, np, jb->d.padangle, wd.data());
         std::vector<T> wt(wd.begin(), wd.end());
         NUDIM_TRY(s.alloc(&s.w, M));
         NUDIM_CUDA(cudaMemcpyAsync(s.w, wt.data(), sizeof(T) * M, cudaMemcpyHostToDevice,
-                                   jb->ctx->stream));
-        NUDIM_CUDA(cudaStreamSynchronize(jb->ctx->stream));
+                                   jb->stream));
     }
     if (jb->d.denoise == NUDIM_DENOISE_TV) {
         NUDIM_TRY(s.alloc(&s.grad, V));
@@ -216,6 +232,7 @@ template <typename T> static int state_init(nudim_job *jb, JobState<T> &s)
     NUDIM_TRY(s.alloc(&s.part, (size_t)nz * s.part_stride + 2 * (size_t)nz + 2));
     NUDIM_TRY(s.alloc(&s.dots, (size_t)nz * 4));
     NUDIM_TRY(s.alloc(&s.rh, (size_t)std::max(1, jb->d.nhio + jb->d.ner)));
+    NUDIM_TRY(s.alloc(&s.it, 1));
     s.live = true;
     return NUDIM_OK;
 }
@@ -240,7 +257,7 @@ template <typename T>
 static int state_setup(nudim_job *jb, JobState<T> &s, const double2 *tomo, const int *d_order,
                        const int *d_rank, const double *d_fill)
 {
-    cudaStream_t st = jb->ctx->stream;
+    cudaStream_t st = jb->stream;
     int nz = jb->d.nz, np = jb->d.np, M = jb->M;
     size_t P2 = (size_t)np * np;
     k_build_slices<T><<<dim3(ceil_div(M, 256), nz), 256, 0, st>>>(
@@ -256,9 +273,13 @@ static int state_setup(nudim_job *jb, JobState<T> &s, const double2 *tomo, const
 }
 
 // One outer HIO/ER iteration nn (reconstruction.c:545-703) on state s.
-template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, int nn)
+// One outer iteration.  Every iteration-dependent value (the R-factor slot,
+// HIO or ER) is read from the device counter s.it, so the same launch
+// sequence can be captured once and replayed (dump = the reference's
+// grad_before/grad_after capture, which copies to the host mid-iteration).
+template <typename T> static int iterate_body(nudim_job *jb, JobState<T> &s, bool dump)
 {
-    cudaStream_t st = jb->ctx->stream;
+    cudaStream_t st = jb->stream;
     const nudim_job_desc &d = jb->d;
     int nz = d.nz, np = d.np, M = jb->M;
     size_t P2 = (size_t)np * np, V = P2 * nz;
@@ -284,7 +305,7 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
     ia.part = s.part;
     ia.part_stride = s.part_stride;
     NUDIM_TRY(s.pl.trafo(nz, pa, ia, st));
-    NUDIM_TRY(launch_finish_r<T>(s.part, s.pl.interp_blocks(), nz, s.part_stride, s.rh, nn, st));
+    NUDIM_TRY(launch_finish_r<T>(s.part, s.pl.interp_blocks(), nz, s.part_stride, s.rh, s.it, st));
     // :587-599 warm start from the real-space plane, CGNR, write back
     CgnrBuffers<T> b = cg_bufs(s);
     NUDIM_TRY(cgnr_run<T>(s.pl, nz, s.y, s.w, s.data, s.img_a, false, iters_of(jb), b, st));
@@ -295,7 +316,6 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
         NUDIM_TRY(launch_unpack<T>(s.data, s.img_b, nz, P2, st));
     }
     // :624-669 denoise
-    bool dump = (nn == jb->dump_nn) && jb->dump_before && d.denoise != NUDIM_DENOISE_NONE;
     if (dump) {
         NUDIM_TRY(launch_to_double<T>(s.img_b, (double *)s.z, V, st));
         NUDIM_CUDA(cudaMemcpyAsync(jb->dump_before, s.z, sizeof(double) * V,
@@ -329,8 +349,50 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
         yhi = (2 * d.ncenter + d.nheight) / 2;
     }
     ProfScope ps(jb->ctx, PK_VOLUME, st, 3.0 * sT * (double)V);
-    NUDIM_TRY(launch_constraint<T>(s.img_b, s.img_a, nz, np, d.nx, nn < d.nhio ? 1 : 0,
+    NUDIM_TRY(launch_constraint<T>(s.img_b, s.img_a, nz, np, d.nx, s.it, d.nhio,
                                    d.height ? 1 : 0, ylo, yhi, st));
+    return NUDIM_OK;
+}
+
+static bool graphs_enabled()
+{
+    const char *e = getenv("NUDIM_GRAPHS");
+    return !(e && e[0] == '0');
+}
+
+// Outer iteration nn (reconstruction.c:545-703).  The first eager run sizes
+// every workspace and plan; later iterations replay a CUDA graph of the
+// same launch sequence (not while profiling or dumping).
+template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, int nn)
+{
+    cudaStream_t st = jb->stream;
+    bool dump = (nn == jb->dump_nn) && jb->dump_before && jb->d.denoise != NUDIM_DENOISE_NONE;
+    NUDIM_TRY(launch_set_counter(s.it, nn, st));
+    bool replay = graphs_enabled() && !dump && !jb->ctx->prof_on;
+    if (replay && s.gexec) {
+        NUDIM_CUDA(cudaGraphLaunch(s.gexec, st));
+        g_launches += s.graph_kernels;  // the library's kernels inside the graph
+        return NUDIM_OK;
+    }
+    NUDIM_TRY(iterate_body<T>(jb, s, dump));
+    if (replay && !s.graph_tried) {
+        s.graph_tried = true;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return NUDIM_OK;
+        }
+        unsigned long long n0 = g_launches;
+        int rc = iterate_body<T>(jb, s, false);
+        s.graph_kernels = g_launches - n0;  // captured, not executed
+        g_launches = n0;
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (rc == NUDIM_OK && e == cudaSuccess && g &&
+            cudaGraphInstantiate(&s.gexec, g, 0) != cudaSuccess)
+            s.gexec = nullptr;
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();  // a failed capture leaves eager execution in place
+    }
     return NUDIM_OK;
 }
 
@@ -338,7 +400,7 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
 // iteration: convert the volume, iterate in FP64, convert back.
 static int corrective_iteration(nudim_job *jb, int nn)
 {
-    cudaStream_t st = jb->ctx->stream;
+    cudaStream_t st = jb->stream;
     size_t V = (size_t)jb->d.np * jb->d.np * jb->d.nz;
     NUDIM_TRY(launch_to_double<float>(jb->s32.img_a, jb->s64.img_a, V, st));
     NUDIM_TRY(state_iterate<double>(jb, jb->s64, nn));
@@ -506,7 +568,19 @@ unsigned long long nudim_launch_count(void) { return g_launches; }
 int nudim_ctx_sync(nudim_ctx *c)
 {
     if (!c) return NUDIM_EINVAL;
-    NUDIM_CUDA(cudaStreamSynchronize(c->stream));
+    NUDIM_CUDA(cudaSetDevice(c->device));
+    // jobs run on their own streams: wait for all work on the device
+    NUDIM_CUDA(cudaDeviceSynchronize());
+    return NUDIM_OK;
+}
+
+void *nudim_job_stream(nudim_job *jb) { return jb ? (void *)jb->stream : nullptr; }
+
+int nudim_job_sync(nudim_job *jb)
+{
+    if (!jb) return NUDIM_EINVAL;
+    NUDIM_CUDA(cudaSetDevice(jb->ctx->device));
+    NUDIM_CUDA(cudaStreamSynchronize(jb->stream));
     return NUDIM_OK;
 }
 
@@ -529,6 +603,21 @@ int nudim_job_create(nudim_ctx *ctx, const nudim_job_desc *desc, nudim_job **out
     NUDIM_CUDA(cudaSetDevice(ctx->device));
     std::unique_ptr<nudim_job> jb(new nudim_job());
     jb->ctx = ctx;
+    NUDIM_CUDA(cudaStreamCreateWithFlags(&jb->stream, cudaStreamNonBlocking));
+    jb->ws.st = jb->stream;
+    // on any early return below, release what was created so far
+    struct Guard {
+        nudim_job *j;
+        ~Guard()
+        {
+            if (!j) return;
+            j->s64.release();
+            j->s32.release();
+            ws_release(&j->ws);
+            cudaStreamSynchronize(j->stream);
+            cudaStreamDestroy(j->stream);
+        }
+    } guard{jb.get()};
     jb->d = *desc;
     nudim_job_desc &d = jb->d;
     jb->nmeas = (int)((d.gam_max - d.gam_min) / d.interval + 0.5) + 1;
@@ -555,20 +644,12 @@ int nudim_job_create(nudim_ctx *ctx, const nudim_job_desc *desc, nudim_job **out
     }
     jb->n_unk_row = cnt;
     if (d.precision == NUDIM_FP64) {
-        int rc = state_init<double>(jb.get(), jb->s64);
-        if (rc) {
-            jb->s64.release();
-            return rc;
-        }
+        NUDIM_TRY(state_init<double>(jb.get(), jb->s64));
     } else {
-        int rc = state_init<float>(jb.get(), jb->s32);
-        if (!rc && d.correct_every > 0) rc = state_init<double>(jb.get(), jb->s64);
-        if (rc) {
-            jb->s32.release();
-            jb->s64.release();
-            return rc;
-        }
+        NUDIM_TRY(state_init<float>(jb.get(), jb->s32));
+        if (d.correct_every > 0) NUDIM_TRY(state_init<double>(jb.get(), jb->s64));
     }
+    guard.j = nullptr;
     *out = jb.release();
     return NUDIM_OK;
 }
@@ -577,9 +658,11 @@ int nudim_job_destroy(nudim_job *jb)
 {
     if (!jb) return NUDIM_OK;
     cudaSetDevice(jb->ctx->device);
-    cudaStreamSynchronize(jb->ctx->stream);
     jb->s64.release();
     jb->s32.release();
+    ws_release(&jb->ws);
+    cudaStreamSynchronize(jb->stream);
+    cudaStreamDestroy(jb->stream);
     delete jb;
     return NUDIM_OK;
 }
@@ -612,7 +695,7 @@ int nudim_job_set_projections(nudim_job *jb, const double *proj, size_t n)
     }
     nudim_ctx *ctx = jb->ctx;
     NUDIM_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t st = ctx->stream;
+    cudaStream_t st = jb->stream;
     // ---- tilt-series NFFT (reconstruction.c:307-367), FP64
     int M1 = d.np * d.nz;
     std::vector<double> x1((size_t)M1 * 2);
@@ -623,18 +706,18 @@ int nudim_job_set_projections(nudim_job *jb, const double *proj, size_t n)
         return NUDIM_EINVAL;
     }
     NfftDev<double> p1;
-    int rc = p1.init(ctx, t1);
+    int rc = p1.init(ctx, t1, st, &jb->ws);
     std::vector<void *> tmp;
     auto talloc = [&](size_t b) -> void * {
         void *q = nullptr;
-        if (cudaMalloc(&q, b) != cudaSuccess) return nullptr;
+        if (cudaMallocAsync(&q, b, st) != cudaSuccess) return nullptr;
         tmp.push_back(q);
         return q;
     };
     auto cleanup = [&]() {
-        cudaStreamSynchronize(st);
-        for (void *q : tmp) cudaFree(q);
+        for (void *q : tmp) cudaFreeAsync(q, st);
         p1.release();
+        cudaStreamSynchronize(st);
     };
     double *d_proj = nullptr;
     double2 *d_fh = nullptr, *d_tomo = nullptr;
@@ -748,7 +831,7 @@ int nudim_job_get_volume(nudim_job *jb, double *out, size_t n, int crop)
         return NUDIM_EINVAL;
     }
     NUDIM_CUDA(cudaSetDevice(jb->ctx->device));
-    cudaStream_t st = jb->ctx->stream;
+    cudaStream_t st = jb->stream;
     std::vector<double> full;
     double *dst = crop ? (full.resize(V), full.data()) : out;
     if (d.precision == NUDIM_FP64) {
@@ -786,7 +869,7 @@ int nudim_job_get_rfactor(nudim_job *jb, double *hist, int cap, int *count)
     int n = std::min(cap, jb->done);
     if (n > 0) {
         NUDIM_CUDA(cudaSetDevice(jb->ctx->device));
-        NUDIM_CUDA(cudaStreamSynchronize(jb->ctx->stream));
+        NUDIM_CUDA(cudaStreamSynchronize(jb->stream));
         double *src = jb->d.precision == NUDIM_FP64 ? jb->s64.rh : jb->s32.rh;
         NUDIM_CUDA(cudaMemcpy(hist, src, sizeof(double) * n, cudaMemcpyDeviceToHost));
     }
@@ -955,6 +1038,8 @@ int nudim_nfft_plan_create(nudim_ctx *ctx, int N0, int N1, int M, const double *
     p->ctx = ctx;
     p->prec = precision;
     int rc = precision == NUDIM_FP64 ? p->d64.init(ctx, t) : p->d32.init(ctx, t);
+    // tables were uploaded on the legacy stream; callers may use any stream
+    if (!rc) rc = cudaStreamSynchronize(nullptr) == cudaSuccess ? NUDIM_OK : NUDIM_ECUDA;
     if (rc) {
         p->d64.release();
         p->d32.release();

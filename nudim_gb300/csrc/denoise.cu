@@ -111,18 +111,42 @@ int tv_run(T *u, T *grad, double *part, int part_cap, double *scal, int nz, int 
 }
 
 // ================================================================ diffusion
-// denoise.c:320-378: per Z-plane, `niter` Gauss-Seidel sweeps in (y, x)
-// order, updated in place.  Cell (y, x) of sweep s reads its N and W
-// neighbours from sweep s and its S and E neighbours from sweep s-1, so the
-// sweeps run as a pipelined anti-diagonal wavefront: at step t sweep s
-// updates diagonal d = t - 2s.  The arithmetic of every cell is the
-// reference's, so the result is bit-identical to the sequential loops.
+// One cell of denoise.c:320-378.  FP64: the reference's 1 / (1 + g^2 / K^2)
+// with IEEE operations in its order (bit-identical).  FP32 form: the same
+// coefficient as K^2 / (K^2 + g^2) with a fast division (relative error a few
+// ulp per cell).
+__device__ __forceinline__ double diff_coef(double g, double Ksq)
+{
+    return rn_div(1.0, rn_add(1.0, rn_div(rn_mul(g, g), Ksq)));
+}
+__device__ __forceinline__ float diff_coef(float g, float Ksq)
+{
+    return __fdividef(Ksq, Ksq + g * g);
+}
+
+template <typename T>
+__device__ __forceinline__ T diff_cell(T cv, T nN, T nS, T nE, T nW, T lambda, T Ksq)
+{
+    T gN = rn_sub(nN, cv), gS = rn_sub(nS, cv), gE = rn_sub(nE, cv), gW = rn_sub(nW, cv);
+    T cN = diff_coef(gN, Ksq), cS = diff_coef(gS, Ksq), cE = diff_coef(gE, Ksq),
+      cW = diff_coef(gW, Ksq);
+    T sum = rn_add(rn_add(rn_add(rn_mul(cN, gN), rn_mul(cS, gS)), rn_mul(cE, gE)),
+                   rn_mul(cW, gW));
+    return rn_add(cv, rn_mul(lambda, sum));
+}
+
+// Per Z-plane, `niter` Gauss-Seidel sweeps in (y, x) order, updated in
+// place.  Cell (y, x) of sweep s reads its N and W neighbours from sweep s
+// and its S and E neighbours from sweep s-1, so the sweeps run as a
+// pipelined anti-diagonal wavefront: at step t sweep s updates diagonal
+// d = t - 2s.  Every cell sees the neighbour values of the sequential loops.
+// This form works in global memory (any plane size).
 template <typename T>
 __global__ void __launch_bounds__(1024)
 k_diffusion(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, int niter)
 {
     T *U = u + (size_t)blockIdx.x * ny * nx;
-    const T lambda = (T)lambda_d, Ksq = (T)ksq_d, one = (T)1;
+    const T lambda = (T)lambda_d, Ksq = (T)ksq_d;
     int D = ny + nx - 1, L = min(ny, nx);
     int nsteps = D + 2 * (niter - 1);
     for (int t = 0; t < nsteps; t++) {
@@ -141,17 +165,101 @@ k_diffusion(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, int ni
             int ip = (x == nxb - 1) ? nxb - 1 : x + 1, im = (x == 0) ? 0 : x - 1;
             T cv = U[(size_t)y * nx + x];
             T e = ip < nx ? U[(size_t)y * nx + ip] : T(0);
-            T gN = rn_sub(U[(size_t)jm * nx + x], cv);
-            T gS = rn_sub(U[(size_t)jp * nx + x], cv);
-            T gE = rn_sub(e, cv);
-            T gW = rn_sub(U[(size_t)y * nx + im], cv);
-            T cN = rn_div(one, rn_add(one, rn_div(rn_mul(gN, gN), Ksq)));
-            T cS = rn_div(one, rn_add(one, rn_div(rn_mul(gS, gS), Ksq)));
-            T cE = rn_div(one, rn_add(one, rn_div(rn_mul(gE, gE), Ksq)));
-            T cW = rn_div(one, rn_add(one, rn_div(rn_mul(gW, gW), Ksq)));
-            T sum = rn_add(rn_add(rn_add(rn_mul(cN, gN), rn_mul(cS, gS)), rn_mul(cE, gE)),
-                           rn_mul(cW, gW));
-            U[(size_t)y * nx + x] = rn_add(cv, rn_mul(lambda, sum));
+            U[(size_t)y * nx + x] = diff_cell<T>(cv, U[(size_t)jm * nx + x],
+                                                 U[(size_t)jp * nx + x], e,
+                                                 U[(size_t)y * nx + im], lambda, Ksq);
+        }
+        __syncthreads();
+    }
+}
+
+// The same wavefront with the live band in shared memory.  Sweeps run in
+// groups of G; inside a group sweep g updates anti-diagonal d = t - 2g at
+// step t, so only diagonals [t - 2G + 1, t + 1] are live: they sit in a ring
+// of R = 2G + 2 diagonal slots (slot = d mod R, cell (y, x) of diagonal d at
+// position y - y0(d)).  During step t diagonal t + 2 is fetched into
+// registers (its slot held diagonal t + 2 - R, written back at step t - 1)
+// and diagonal t - 2G + 1, final for the group, is written back: one barrier
+// per step.  Requires min(ny, nx) <= kDiffPf * blockDim.x.
+constexpr int kDiffPf = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(1024)
+k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, int niter,
+                 int G, int R)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *ring = (T *)smraw;
+    T *U = u + (size_t)blockIdx.x * ny * nx;
+    const T lambda = (T)lambda_d, Ksq = (T)ksq_d;
+    const int D = ny + nx - 1, L = min(ny, nx);
+    const int P = min((int)blockDim.x, (L + 31) & ~31), gs = blockDim.x / P;
+    const int gi = threadIdx.x / P, i0 = threadIdx.x - gi * P;
+    auto y0 = [&](int d) { return max(0, d - (nx - 1)); };
+    auto len = [&](int d) { return min(d, ny - 1) - y0(d) + 1; };
+    auto slot = [&](int d) { return ring + (size_t)(d % R) * L; };
+    auto cell = [&](int d, int i) -> size_t {
+        int a = y0(d);
+        return (size_t)(a + i) * nx + (d - a - i);
+    };
+    for (int s0 = 0; s0 < niter; s0 += G) {
+        const int gc = min(G, niter - s0);
+        const int nsteps = D + 2 * (gc - 1);
+        for (int d = 0; d < 2 && d < D; d++) {
+            T *s = slot(d);
+            for (int i = threadIdx.x; i < len(d); i += blockDim.x) s[i] = U[cell(d, i)];
+        }
+        __syncthreads();
+        for (int t = 0; t < nsteps; t++) {
+            // fetch diagonal t + 2
+            const int dn = t + 2;
+            const int nn = dn < D ? len(dn) : 0;
+            T pf[kDiffPf];
+#pragma unroll
+            for (int k = 0; k < kDiffPf; k++) {
+                int i = threadIdx.x + k * blockDim.x;
+                pf[k] = i < nn ? U[cell(dn, i)] : T(0);
+            }
+            int g_hi = min(gc - 1, t / 2);
+            int a = t - (D - 1);
+            int g_lo = a > 0 ? (a + 1) / 2 : 0;
+            // P threads per diagonal, gs diagonals at a time
+            for (int g = g_lo + gi; gi < gs && g <= g_hi; g += gs) {
+                const int d = t - 2 * g;
+                const int yd = y0(d), nd = len(d);
+                const int ym = y0(d > 0 ? d - 1 : d), yp = y0(d + 1);
+                T *sc = slot(d);
+                const T *sm = slot(d > 0 ? d - 1 : d), *sp = slot(d + 1);
+                for (int i = i0; i < nd; i += P) {
+                    int y = yd + i, x = d - y;
+                    T cv = sc[i];
+                    T nN = cv, nS = cv, nW = cv, nE = cv;
+                    if (y > 0) nN = sm[(y - 1) - ym];
+                    if (x > 0) nW = sm[y - ym];
+                    if (y < ny - 1) nS = sp[(y + 1) - yp];
+                    int ip = (x == nxb - 1) ? nxb - 1 : x + 1;
+                    if (ip != x) nE = ip < nx ? sp[y - yp] : T(0);
+                    sc[i] = diff_cell<T>(cv, nN, nS, nE, nW, lambda, Ksq);
+                }
+            }
+            if (nn > 0) {
+                T *s = slot(dn);
+#pragma unroll
+                for (int k = 0; k < kDiffPf; k++) {
+                    int i = threadIdx.x + k * blockDim.x;
+                    if (i < nn) s[i] = pf[k];
+                }
+            }
+            const int df = t - 2 * gc + 1;  // final for this group
+            if (df >= 0 && df < D) {
+                const T *s = slot(df);
+                for (int i = threadIdx.x; i < len(df); i += blockDim.x) U[cell(df, i)] = s[i];
+            }
+            __syncthreads();
+        }
+        {
+            const T *s = slot(D - 1);
+            for (int i = threadIdx.x; i < len(D - 1); i += blockDim.x) U[cell(D - 1, i)] = s[i];
         }
         __syncthreads();
     }
@@ -163,7 +271,26 @@ int diffusion_run(T *u, int nz, int ny, int nx, int nx_bound, float lambda, floa
 {
     if (niter <= 0 || nz <= 0) return NUDIM_OK;
     double ksq = (double)kappa * (double)kappa;
-    k_diffusion<T><<<nz, 1024, 0, st>>>(u, ny, nx, nx_bound, (double)lambda, ksq, niter);
+    int L = ny < nx ? ny : nx;
+    int P = std::min(1024, (L + 31) & ~31);
+    // FP32 on planes up to 512 wide: two diagonals at a time, two CTAs per
+    // SM; otherwise one CTA of 1024 threads with up to 160 KB of ring
+    bool two = sizeof(T) == 4 && P <= 512;
+    int threads = two ? 2 * P : 1024;
+    const size_t budget = two ? ((size_t)110 << 10) : ((size_t)160 << 10);
+    int G = (int)((budget / (sizeof(T) * (size_t)L) - 2) / 2);
+    if (G > niter) G = niter;
+    if (G >= 1 && L <= kDiffPf * threads) {
+        int R = 2 * G + 2;
+        size_t smem = sizeof(T) * (size_t)R * L;
+        NUDIM_CUDA(cudaFuncSetAttribute(k_diffusion_ring<T>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        160 << 10));
+        k_diffusion_ring<T><<<nz, threads, smem, st>>>(u, ny, nx, nx_bound, (double)lambda, ksq,
+                                                        niter, G, R);
+    } else {
+        k_diffusion<T><<<nz, 1024, 0, st>>>(u, ny, nx, nx_bound, (double)lambda, ksq, niter);
+    }
     NUDIM_LAUNCH_CHECK();
     return NUDIM_OK;
 }

@@ -63,6 +63,16 @@ struct nudim_ctx {
 
 namespace nudim {
 
+// Stream-ordered scratch owned by one stream (a job or the context): grows
+// with cudaFreeAsync/cudaMallocAsync on that stream, never syncs the device.
+struct Workspace {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaStream_t st = nullptr;
+};
+int ws_get(Workspace *w, size_t bytes, void **out);
+void ws_release(Workspace *w);
+
 // Times the launches issued on `st` while it lives (one record per scope);
 // `bytes` is the algorithmic traffic the scope's launches move.
 struct ProfScope {
@@ -77,6 +87,7 @@ struct ProfScope {
 int prof_collect(nudim_ctx *c);
 
 int ctx_workspace(nudim_ctx *ctx, size_t bytes, void **p);
+int upload_async(void **dst, const void *src, size_t nb, cudaStream_t st);
 int ctx_scratch(nudim_ctx *ctx, size_t bytes, double **p);
 int ctx_fft2d(nudim_ctx *ctx, int n0, int n1, int batch, int prec, cufftHandle *h);
 
@@ -136,6 +147,8 @@ template <typename T> struct CropArgs {
 template <typename T> struct NfftDev {
     using C = cplx_t<T>;
     nudim_ctx *ctx = nullptr;
+    Workspace *wsp = nullptr;  // scratch of the owning stream (nullptr: context's)
+    cudaStream_t ast = nullptr;  // stream the tables were allocated on
     int N0 = 0, N1 = 0, n0 = 0, n1 = 0, M = 0;
     int ty = 16, tx = 16, nty = 0, ntx = 0;
     int2 *u = nullptr;
@@ -146,14 +159,20 @@ template <typename T> struct NfftDev {
 
     // fused path (nfft_fused.cu): no oversampled grid in HBM
     bool fused = false;
-    int BC = 0, nblk = 0, smax = 0, rows = 4;
+    int BC = 0, nblk = 0, smax = 0, rows = 4;    // trafo column blocks
+    int BCa = 0, nblka = 0, nbands = 0, Pa = 1;  // adjoint column blocks, planes per CTA
+    size_t smem_col = 0, smem_row = 0, smem_spread = 0;
     C *tw0 = nullptr, *tw1 = nullptr;
-    int *blk_off = nullptr, *ent = nullptr, *band_row = nullptr, *band_off = nullptr,
-        *band_node = nullptr;
+    int *blk_off = nullptr, *ent = nullptr, *band_off = nullptr, *band_node = nullptr,
+        *band_ord = nullptr;
+    T *band_w = nullptr;            // per adjoint tile entry: R row + BCa column weights
     unsigned char *nslots = nullptr;
 
-    int init(nudim_ctx *c, const NfftTables &t);
+    // uploads go on stream st (tables are consumed by later work on st)
+    int init(nudim_ctx *c, const NfftTables &t, cudaStream_t st = nullptr,
+             Workspace *w = nullptr);
     void release();
+    int workspace(size_t bytes, void **p);
     int chunk_for(int nplanes) const;
     int interp_blocks() const { return ceil_div(M, 256); }
     int crop_blocks() const
@@ -163,7 +182,7 @@ template <typename T> struct NfftDev {
     int trafo(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia, cudaStream_t st);
     int adjoint(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca, cudaStream_t st);
 
-    int init_fused(const NfftTables &t);
+    int init_fused(const NfftTables &t, cudaStream_t st);
     void release_fused();
     int fused_chunk(int nplanes) const;
     int trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia, cudaStream_t st);
@@ -171,7 +190,6 @@ template <typename T> struct NfftDev {
                       cudaStream_t st);
 };
 
-constexpr int kFusedWarps = 16;  // warps (and spreading row bands) per column-block CTA
 
 // CGNR over `nplanes` planes (solver_before_loop + iters x loop_one_step).
 // f: planes of N0*N1 (start value in, result out), y/r/v: planes of M,
@@ -197,11 +215,12 @@ int launch_pack(const T *img, cplx_t<T> *data, int nz, size_t P2, cudaStream_t s
 template <typename T>
 int launch_unpack(const cplx_t<T> *data, T *img, int nz, size_t P2, cudaStream_t st);
 template <typename T>
-int launch_constraint(T *img, const T *img_last, int nz, int np, int nx, int hio, int height,
-                      int ylo, int yhi, cudaStream_t st);
+int launch_constraint(T *img, const T *img_last, int nz, int np, int nx, const int *it,
+                      int nhio, int height, int ylo, int yhi, cudaStream_t st);
 template <typename T>
 int launch_finish_r(const double *part, int nparts, int nplanes, int stride, double *rh,
-                    int nn, cudaStream_t st);
+                    const int *it, cudaStream_t st);
+int launch_set_counter(int *it, int v, cudaStream_t st);
 template <typename T>
 int launch_real_to(const double *src, T *dst, size_t n, cudaStream_t st);
 template <typename T>

@@ -172,9 +172,21 @@ void launch_finish_sums(const double *part, int nparts, int nplanes, int stride_
 }
 
 // ================================================================ plan setup
-template <typename T> int NfftDev<T>::init(nudim_ctx *c, const NfftTables &t)
+// Stream-ordered upload of a host array (pageable sources are staged before
+// cudaMemcpyAsync returns, so the host copy may be released right after).
+int upload_async(void **dst, const void *src, size_t nb, cudaStream_t st)
+{
+    NUDIM_CUDA(cudaMallocAsync(dst, nb ? nb : 8, st));
+    if (nb) NUDIM_CUDA(cudaMemcpyAsync(*dst, src, nb, cudaMemcpyHostToDevice, st));
+    return NUDIM_OK;
+}
+
+template <typename T>
+int NfftDev<T>::init(nudim_ctx *c, const NfftTables &t, cudaStream_t st, Workspace *w)
 {
     ctx = c;
+    wsp = w;
+    ast = st;
     N0 = t.N0;
     N1 = t.N1;
     n0 = t.n0;
@@ -189,37 +201,54 @@ template <typename T> int NfftDev<T>::init(nudim_ctx *c, const NfftTables &t)
     std::vector<T> hp(t.psi.begin(), t.psi.end());
     std::vector<T> hc0(t.c0.begin(), t.c0.end()), hc1(t.c1.begin(), t.c1.end());
     size_t nb_u = sizeof(int2) * (size_t)M, nb_p = sizeof(T) * hp.size();
-    NUDIM_CUDA(cudaMalloc(&u, nb_u > 0 ? nb_u : 8));
-    NUDIM_CUDA(cudaMalloc(&psi, nb_p > 0 ? nb_p : 8));
-    NUDIM_CUDA(cudaMalloc(&c0, sizeof(T) * N0));
-    NUDIM_CUDA(cudaMalloc(&c1, sizeof(T) * N1));
-    NUDIM_CUDA(cudaMalloc(&tile_off, sizeof(int) * t.tile_off.size()));
-    NUDIM_CUDA(cudaMalloc(&tile_nodes, sizeof(int) * (t.tile_nodes.size() + 1)));
-    if (M) NUDIM_CUDA(cudaMemcpy(u, hu.data(), nb_u, cudaMemcpyHostToDevice));
-    if (M) NUDIM_CUDA(cudaMemcpy(psi, hp.data(), nb_p, cudaMemcpyHostToDevice));
-    NUDIM_CUDA(cudaMemcpy(c0, hc0.data(), sizeof(T) * N0, cudaMemcpyHostToDevice));
-    NUDIM_CUDA(cudaMemcpy(c1, hc1.data(), sizeof(T) * N1, cudaMemcpyHostToDevice));
-    NUDIM_CUDA(cudaMemcpy(tile_off, t.tile_off.data(), sizeof(int) * t.tile_off.size(),
-                          cudaMemcpyHostToDevice));
-    if (!t.tile_nodes.empty())
-        NUDIM_CUDA(cudaMemcpy(tile_nodes, t.tile_nodes.data(),
-                              sizeof(int) * t.tile_nodes.size(), cudaMemcpyHostToDevice));
-    bytes = nb_u + nb_p + sizeof(T) * (N0 + N1) +
-            sizeof(int) * (t.tile_off.size() + t.tile_nodes.size());
-    // pageable uploads may still be in flight when cudaMemcpy returns
-    NUDIM_CUDA(cudaDeviceSynchronize());
-    if (c->use_fused) return init_fused(t);
+    NUDIM_TRY(upload_async((void **)&u, hu.data(), nb_u, st));
+    NUDIM_TRY(upload_async((void **)&psi, hp.data(), nb_p, st));
+    NUDIM_TRY(upload_async((void **)&c0, hc0.data(), sizeof(T) * N0, st));
+    NUDIM_TRY(upload_async((void **)&c1, hc1.data(), sizeof(T) * N1, st));
+    bytes = nb_u + nb_p + sizeof(T) * (N0 + N1);
+    // the fused path serves every geometry but extremely narrow grids, which
+    // take the grid path below
+    if (c->use_fused && init_fused(t, st) == NUDIM_OK) return NUDIM_OK;
+    fused = false;
+    // grid path: tile lists of the spreading gather
+    NUDIM_TRY(upload_async((void **)&tile_off, t.tile_off.data(),
+                           sizeof(int) * t.tile_off.size(), st));
+    NUDIM_TRY(upload_async((void **)&tile_nodes, t.tile_nodes.data(),
+                           sizeof(int) * t.tile_nodes.size(), st));
+    bytes += sizeof(int) * (t.tile_off.size() + t.tile_nodes.size());
     return NUDIM_OK;
+}
+
+template <typename T> int NfftDev<T>::workspace(size_t nb, void **p)
+{
+    return wsp ? ws_get(wsp, nb, p) : ctx_workspace(ctx, nb, p);
+}
+
+int ws_get(Workspace *w, size_t bytes, void **out)
+{
+    if (bytes > w->bytes) {
+        if (w->p) NUDIM_CUDA(cudaFreeAsync(w->p, w->st));
+        w->p = nullptr;
+        w->bytes = 0;
+        NUDIM_CUDA(cudaMallocAsync(&w->p, bytes, w->st));
+        w->bytes = bytes;
+    }
+    *out = w->p;
+    return NUDIM_OK;
+}
+
+void ws_release(Workspace *w)
+{
+    if (w->p) cudaFreeAsync(w->p, w->st);
+    w->p = nullptr;
+    w->bytes = 0;
 }
 
 template <typename T> void NfftDev<T>::release()
 {
-    cudaFree(u);
-    cudaFree(psi);
-    cudaFree(c0);
-    cudaFree(c1);
-    cudaFree(tile_off);
-    cudaFree(tile_nodes);
+    void *ptrs[] = {u, psi, c0, c1, tile_off, tile_nodes};
+    for (void *q : ptrs)
+        if (q) cudaFreeAsync(q, ast);
     u = nullptr;
     psi = nullptr;
     c0 = c1 = nullptr;
@@ -440,7 +469,7 @@ int NfftDev<T>::trafo(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia
     if (fused) return trafo_fused(nplanes, pa, ia, st);
     int chunk = chunk_for(nplanes);
     void *wsv;
-    NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (size_t)n0 * n1 * chunk, &wsv));
+    NUDIM_TRY(workspace(sizeof(C) * (size_t)n0 * n1 * chunk, &wsv));
     C *grid = (C *)wsv;
     size_t cells = (size_t)n0 * n1;
     const double c = sizeof(C), tab = (double)M * (8 + 2 * kW * sizeof(T));
@@ -488,7 +517,7 @@ int NfftDev<T>::adjoint(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> 
     if (fused) return adjoint_fused(nplanes, sa, ca, st);
     int chunk = chunk_for(nplanes);
     void *wsv;
-    NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (size_t)n0 * n1 * chunk, &wsv));
+    NUDIM_TRY(workspace(sizeof(C) * (size_t)n0 * n1 * chunk, &wsv));
     C *grid = (C *)wsv;
     const double c = sizeof(C), cells = (double)n0 * n1,
                  tab = (double)M * (8 + 2 * kW * sizeof(T));

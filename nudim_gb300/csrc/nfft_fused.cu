@@ -18,6 +18,8 @@
 //
 // No atomics: every output element has exactly one writer, and every sum
 // has a fixed order, so results are deterministic.
+#include <type_traits>
+
 #include "engine.cuh"
 
 namespace nudim {
@@ -139,10 +141,19 @@ k_rowfft(const void *__restrict__ src, size_t src_stride, int N0, int N1, int n1
 }
 
 // ================================================================ K2 column pass + interpolation
+// warps per trafo column-block CTA (FP64: fewer, with room for the row weights)
+template <typename T> __host__ __device__ constexpr int col_warps() { return sizeof(T) == 4 ? 32 : 16; }
+
+// Shared memory: two BC x n0 complex buffers (FFT).  After the column FFTs
+// each lane takes one (node, block) entry of the block's list and sums the
+// node's window over the block's columns: for each of the cnt columns
+// inside the window, the 14-row column sum weighted by psi0, then weighted
+// by the column's psi1.  The list holds entries with equal cnt side by side,
+// so the lanes of a warp run loops of equal length.
 template <typename T>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(32 * col_warps<T>(), 1)
 k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int n1, int BC,
-                const cplx_t<T> *__restrict__ tw0, const int2 *__restrict__ u,
+                int nblk, const cplx_t<T> *__restrict__ tw0, const int2 *__restrict__ u,
                 const T *__restrict__ psi, const int *__restrict__ blk_off,
                 const int *__restrict__ ent, int M, int smax, cplx_t<T> *__restrict__ part)
 {
@@ -152,6 +163,7 @@ k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int 
     int cb = blockIdx.x, b = blockIdx.y;
     const C *Hb = H + (size_t)b * N0 * n1 + (size_t)cb * BC;
     // rows a of H land at l0 = (a - N0/2) mod n0; the other rows are zero
+#pragma unroll 4
     for (int idx = threadIdx.x; idx < n0 * BC; idx += blockDim.x) {
         int l0 = idx / BC, c = idx - l0 * BC;
         int k0 = l0 < n0 / 2 ? l0 : l0 - n0;
@@ -160,46 +172,49 @@ k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int 
         A[(size_t)c * n0 + l0] = v;
     }
     __syncthreads();
-    C *G = block_fft<T, -1>(A, B, n0, logn0, BC, tw0);
-    // half-warp per (node, block) entry
-    int lane = threadIdx.x & 31, t0 = lane & 15;
-    int hw = threadIdx.x >> 4, nhw = blockDim.x >> 4;
-    int beg = blk_off[cb], end = blk_off[cb + 1];
-    int col0 = cb * BC;
-    for (int e0 = beg; e0 < end; e0 += nhw) {
-        int e = e0 + hw;
+    const C *G = block_fft<T, -1>(A, B, n0, logn0, BC, tw0);
+    const int beg = blk_off[cb], end = blk_off[cb + 1];
+    const int col0 = cb * BC, m0 = n0 - 1;
+    for (int e = beg + threadIdx.x; e < end; e += blockDim.x) {
+        const int en = ent[e], j = en >> 3;
+        const int2 uu = u[j];
+        const T *ps = psi + (size_t)j * 2 * kW;
+        // the row weights as 16-byte vectors (a psi row is 2 kW = 28
+        // values: 112 or 224 bytes, so every row starts 16-byte aligned)
+        using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+        constexpr int TV = sizeof(V) / sizeof(T), NV = (kW + TV - 1) / TV;
+        T q0[NV * TV];
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+            V x = ((const V *)ps)[i];
+            memcpy(&q0[i * TV], &x, sizeof(V));
+        }
+        // the window's columns inside this block: cnt columns from block
+        // column cl0 (window column t1lo); one block: all kW, wrapping
+        int t1lo = 0, cl0 = 0, cnt = kW;
+        if (nblk > 1) {
+            int dd = (col0 - uu.y) & (n1 - 1);
+            if (dd < kW) t1lo = dd;
+            else cl0 = (uu.y - col0) & (n1 - 1);
+            cnt = min(kW - t1lo, BC - cl0);
+        }
         T ar = 0, ai = 0;
-        int j = 0, slot = 0;
-        bool valid = e < end;
-        if (valid) {
-            int en = ent[e];
-            j = en >> 3;
-            slot = en & 7;
-            if (t0 < kW) {
-                int2 uu = u[j];
-                const T *ps = psi + (size_t)j * 2 * kW;
-                int r = (uu.x + t0) & (n0 - 1);
+        for (int q = 0; q < cnt; q++) {
+            int t1 = t1lo + q;
+            int cl = nblk > 1 ? cl0 + q : ((uu.y + t1) & (n1 - 1));
+            const C *gp = G + (size_t)cl * n0;
+            T sr = 0, si = 0;
 #pragma unroll
-                for (int t1 = 0; t1 < kW; t1++) {
-                    int cl = ((uu.y + t1) & (n1 - 1)) - col0;
-                    if (cl >= 0 && cl < BC) {
-                        C g = G[(size_t)cl * n0 + r];
-                        T q1 = ps[kW + t1];
-                        ar += q1 * g.x;
-                        ai += q1 * g.y;
-                    }
-                }
-                T q0 = ps[t0];
-                ar *= q0;
-                ai *= q0;
+            for (int t = 0; t < kW; t++) {
+                C g = gp[(uu.x + t) & m0];
+                sr += q0[t] * g.x;
+                si += q0[t] * g.y;
             }
+            T w = ps[kW + t1];
+            ar += w * sr;
+            ai += w * si;
         }
-#pragma unroll
-        for (int o = 8; o > 0; o >>= 1) {
-            ar += __shfl_xor_sync(0xffffffffu, ar, o, 16);
-            ai += __shfl_xor_sync(0xffffffffu, ai, o, 16);
-        }
-        if (valid && t0 == 0) part[((size_t)b * smax + slot) * M + j] = mkc<T>(ar, ai);
+        part[((size_t)b * smax + (en & 7)) * M + j] = mkc<T>(ar, ai);
     }
 }
 
@@ -255,79 +270,151 @@ k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ 
 }
 
 // ================================================================ K4 spread + column IFFT
-template <typename T, bool WEIGHTED>
-__global__ void __launch_bounds__(512)
-k_spread_colifft(SpreadArgs<T> sa, const int2 *__restrict__ u, const T *__restrict__ psi,
-                 const int *__restrict__ band_row, const int *__restrict__ band_off,
-                 const int *__restrict__ band_node, int W, int N0, int n0, int logn0, int n1,
-                 int BC, const cplx_t<T> *__restrict__ tw0, int plane0,
+// Gather form over P planes at once: warp w takes tiles of R = 32/BC rows x
+// BC columns of the block (one grid point per lane), longest list first,
+// from a shared counter, and sums for its point and each of the P planes
+// the contributions of the tile's node list in ascending node order -- the
+// per-point order of the grid path.  Each list entry carries the tile's
+// window weights (R row weights, BC column weights, zero outside the
+// window), so a node costs a lane two weight reads, one product and two
+// FMAs per plane.  FP32: plain sums within a batch of kStage nodes,
+// compensated (Neumaier) sums across batches.  The tile sums go to S_p;
+// then per plane n0-point inverse FFTs of the BC columns.
+// Shared memory: S_0..S_{P-1}, K (BC x n0 complex each; K is FFT scratch),
+// then the warps' node stages.
+constexpr int kSpreadWarps = 16;
+constexpr int kMaxBands = 1024;
+
+template <typename T> __host__ __device__ constexpr int spread_batch() { return sizeof(T) == 4 ? 16 : 8; }
+
+// stage of one warp: weights [NB][W] (W = R + BC = 12 for BC = 4), node values [P][NB]
+template <typename T, int P> __host__ __device__ constexpr size_t spread_stage_bytes(int W)
+{
+    return (size_t)spread_batch<T>() * (W * sizeof(T) + P * sizeof(cplx_t<T>));
+}
+
+template <typename T, bool WEIGHTED, int P>
+__global__ void __launch_bounds__(32 * kSpreadWarps, 1)
+k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
+                 const int *__restrict__ band_ord, const int *__restrict__ band_node,
+                 const T *__restrict__ band_w, int nbands, int N0, int n0, int logn0, int n1,
+                 int BC, int nb_planes, const cplx_t<T> *__restrict__ tw0, int plane0,
                  cplx_t<T> *__restrict__ Hp)
 {
     using C = cplx_t<T>;
+    constexpr int NB = spread_batch<T>();
     extern __shared__ __align__(16) unsigned char smraw[];
-    C *S = (C *)smraw, *K = S + (size_t)BC * n0;  // sums and compensations (FFT scratch)
-    int cb = blockIdx.x, b = blockIdx.y, gb = plane0 + b;
-    for (int i = threadIdx.x; i < 2 * BC * n0; i += blockDim.x) S[i] = mkc<T>(0, 0);
+    __shared__ int next_tile, s_off[kMaxBands + 1], s_ord[kMaxBands];
+    const size_t buf = (size_t)BC * n0;
+    C *S = (C *)smraw, *K = S + P * buf;
+    const int cb = blockIdx.x, pb = blockIdx.y * P;
+    const int np = min(P, nb_planes - pb);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const int R = 32 / BC, W = R + BC;
+    unsigned char *wst = (unsigned char *)(K + buf) + warp * spread_stage_bytes<T, P>(W);
+    T *ws = (T *)wst;                  // [NB][W]
+    C *fs = (C *)(ws + NB * W);        // [P][NB]
+    const int rr = lane / BC, cc = lane - rr * BC;
+    for (int i = threadIdx.x; i <= nbands; i += blockDim.x) {
+        s_off[i] = band_off[(size_t)cb * nbands + i];
+        if (i < nbands) s_ord[i] = band_ord[(size_t)cb * nbands + i];
+    }
+    if (threadIdx.x == 0) next_tile = nwarps;
     __syncthreads();
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const C *f = sa.f + (size_t)gb * sa.f_stride;
-    int col0 = cb * BC;
-    for (int w = warp; w < W; w += blockDim.x >> 5) {
-        int rlo = band_row[cb * (W + 1) + w], rhi = band_row[cb * (W + 1) + w + 1];
-        int beg = band_off[cb * W + w], end = band_off[cb * W + w + 1];
-        for (int e = beg; e < end; e++) {
-            int j = band_node[e];
-            int2 uu = u[j];
-            C fv = f[j];
-            if (WEIGHTED) {
-                T wv = sa.w[j];
-                fv = mkc<T>(wv * fv.x, wv * fv.y);
-            }
-            T my = lane < 2 * kW ? psi[(size_t)j * 2 * kW + lane] : T(0);
-            // every lane runs the same number of iterations: the shuffles
-            // below need all 32 lanes each time
-            for (int qb = 0; qb < kW * kW; qb += 32) {
-                int q = qb + lane;
-                int t0 = q / kW, t1 = q - t0 * kW;
-                T q0 = __shfl_sync(0xffffffffu, my, t0 < kW ? t0 : 0);
-                T q1 = __shfl_sync(0xffffffffu, my, kW + t1);
-                if (q < kW * kW) {
-                    int r = (uu.x + t0) & (n0 - 1);
-                    int cl = ((uu.y + t1) & (n1 - 1)) - col0;
-                    if (r >= rlo && r < rhi && cl >= 0 && cl < BC) {
-                        T vr = q1 * (q0 * fv.x), vi = q1 * (q0 * fv.y);
-                        size_t o = (size_t)cl * n0 + r;
-                        C sv = S[o];
-                        if (sizeof(T) == 4) {
-                            // Neumaier-compensated accumulation
-                            C kv = K[o];
-                            T tr = sv.x + vr, ti = sv.y + vi;
-                            kv.x += fabs(sv.x) >= fabs(vr) ? (sv.x - tr) + vr : (vr - tr) + sv.x;
-                            kv.y += fabs(sv.y) >= fabs(vi) ? (sv.y - ti) + vi : (vi - ti) + sv.y;
-                            S[o] = mkc<T>(tr, ti);
-                            K[o] = kv;
-                        } else {
-                            S[o] = mkc<T>(sv.x + vr, sv.y + vi);
-                        }
+    // weights of a batch move as 16-byte vectors
+    using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    constexpr int TV = sizeof(V) / sizeof(T);
+    for (int it = warp; it < nbands;) {
+        const int v = s_ord[it];
+        const int r = v * R + rr;
+        const int beg = s_off[v], end = s_off[v + 1];
+        T ar[P], ai[P];
+        Comp<T> kr[P], ki[P];
+#pragma unroll
+        for (int p = 0; p < P; p++) {
+            ar[p] = ai[p] = T(0);
+            kr[p].init();
+            ki[p].init();
+        }
+        for (int base = beg; base < end; base += NB) {
+            const int n = min(NB, end - base);
+            // node values (zero past the list end)
+            if (lane < NB) {
+                int jl = lane < n ? band_node[base + lane] : 0;
+                T wv = (WEIGHTED && lane < n) ? sa.w[jl] : T(1);
+#pragma unroll
+                for (int p = 0; p < P; p++) {
+                    C fv = mkc<T>(0, 0);
+                    if (lane < n && p < np) {
+                        fv = sa.f[(size_t)(plane0 + pb + p) * sa.f_stride + jl];
+                        if (WEIGHTED) fv = mkc<T>(wv * fv.x, wv * fv.y);
                     }
+                    fs[p * NB + lane] = fv;
+                }
+            }
+            // weights (zero past the list end)
+            const V *src = (const V *)(band_w + (size_t)base * W);
+            for (int q = lane; q < NB * W / TV; q += 32) {
+                V val;
+                if (q * TV < n * W) val = src[q];
+                else memset(&val, 0, sizeof(V));
+                ((V *)ws)[q] = val;
+            }
+            __syncwarp();
+            T br[P], bi[P];
+#pragma unroll
+            for (int p = 0; p < P; p++) br[p] = bi[p] = T(0);
+#pragma unroll
+            for (int k = 0; k < NB; k++) {
+                T q0 = ws[k * W + rr], q1 = ws[k * W + R + cc];
+                if (sizeof(T) == 4) {
+                    T q = q0 * q1;
+#pragma unroll
+                    for (int p = 0; p < P; p++) {
+                        C fv = fs[p * NB + k];
+                        br[p] += q * fv.x;
+                        bi[p] += q * fv.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int p = 0; p < P; p++) {
+                        C fv = fs[p * NB + k];
+                        ar[p] += q1 * (q0 * fv.x);
+                        ai[p] += q1 * (q0 * fv.y);
+                    }
+                }
+            }
+            if (sizeof(T) == 4) {
+#pragma unroll
+                for (int p = 0; p < P; p++) {
+                    kr[p].add(br[p]);
+                    ki[p].add(bi[p]);
                 }
             }
             __syncwarp();
         }
+#pragma unroll
+        for (int p = 0; p < P; p++) {
+            if (sizeof(T) == 4) {
+                ar[p] = kr[p].value();
+                ai[p] = ki[p].value();
+            }
+            S[p * buf + (size_t)cc * n0 + r] = mkc<T>(ar[p], ai[p]);
+        }
+        int nv = 0;
+        if (lane == 0) nv = atomicAdd(&next_tile, 1);
+        it = __shfl_sync(0xffffffffu, nv, 0);
     }
     __syncthreads();
-    if (sizeof(T) == 4)
-        for (int i = threadIdx.x; i < BC * n0; i += blockDim.x) {
-            C sv = S[i], kv = K[i];
-            S[i] = mkc<T>(sv.x + kv.x, sv.y + kv.y);
+    for (int p = 0; p < np; p++) {
+        C *G = block_fft<T, +1>(S + p * buf, K, n0, logn0, BC, tw0);
+        C *Hb = Hp + (size_t)(pb + p) * N0 * n1 + cb * BC;
+        for (int idx = threadIdx.x; idx < N0 * BC; idx += blockDim.x) {
+            int a = idx / BC, cl = idx - a * BC;
+            int l0 = (a - N0 / 2) & (n0 - 1);
+            Hb[(size_t)a * n1 + cl] = G[(size_t)cl * n0 + l0];
         }
-    __syncthreads();
-    C *G = block_fft<T, +1>(S, K, n0, logn0, BC, tw0);
-    C *Hb = Hp + (size_t)b * N0 * n1 + col0;
-    for (int idx = threadIdx.x; idx < N0 * BC; idx += blockDim.x) {
-        int a = idx / BC, c = idx - a * BC;
-        int l0 = (a - N0 / 2) & (n0 - 1);
-        Hb[(size_t)a * n1 + c] = G[(size_t)c * n0 + l0];
+        __syncthreads();
     }
 }
 
@@ -375,7 +462,7 @@ static int ilog2(int n)
     return l;
 }
 
-template <typename T> int NfftDev<T>::init_fused(const NfftTables &t)
+template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream_t st)
 {
     // column-block width: two BC x n0 complex buffers within 128 KB
     int bc = (int)((128 << 10) / (2 * sizeof(C) * (size_t)t.n0));
@@ -385,74 +472,108 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t)
     while (p * 2 <= bc) p *= 2;
     bc = p;
     if (bc < 1) return NUDIM_EINVAL;
+    // a window must not wrap onto its own block: narrow grids use one block
+    if (t.n1 < kW - 1 + bc && t.n1 <= 32 && 2 * sizeof(C) * (size_t)t.n1 * t.n0 <= (128u << 10))
+        bc = t.n1;
+    // adjoint: blocks of 4 columns (tiles of 8 x 4 grid points; the tile's
+    // 12 weights move as 16-byte vectors)
+    if (t.n1 < 4 || t.n0 < 8) return NUDIM_EINVAL;
+    const int bca = 4;
     FusedLists L;
-    if (build_fused_lists(t, bc, kFusedWarps, &L) != 0) {
+    if (build_fused_lists(t, bc, bca, &L) != 0) {
         set_error("fused NFFT list construction failed");
         return NUDIM_EINVAL;
     }
     BC = L.BC;
     nblk = L.nblk;
     smax = L.smax;
+    BCa = L.BCa;
+    nblka = L.nblka;
+    nbands = L.nbands;
+    if (nbands > kMaxBands) return NUDIM_EINVAL;
     // rows per CTA in the row passes: two rows x n1 complex buffers within 112 KB
     rows = (int)((112 << 10) / (2 * sizeof(C) * (size_t)t.n1));
     if (rows > 4) rows = 4;
+    smem_col = 2 * sizeof(C) * (size_t)BC * n0;
+    smem_row = 2 * sizeof(C) * (size_t)rows * n1;
+    // adjoint column pass: as many planes per CTA (4, 2, 1) as fit in 212 KB
+    // of dynamic shared memory (8 KB of tile offsets and order are static)
+    const int Wa = 32 / BCa + BCa;
+    size_t bufa = sizeof(C) * (size_t)BCa * n0;
+    auto spread_smem = [&](int p) -> size_t {
+        size_t st = p == 4 ? spread_stage_bytes<T, 4>(Wa)
+                  : p == 2 ? spread_stage_bytes<T, 2>(Wa) : spread_stage_bytes<T, 1>(Wa);
+        return (p + 1) * bufa + kSpreadWarps * st;
+    };
+    Pa = 4;
+    while (Pa > 1 && spread_smem(Pa) > ((size_t)212 << 10)) Pa /= 2;
+    smem_spread = spread_smem(Pa);
+    // The limit is a property of the kernel, shared by every plan in the
+    // process: set it to the largest size any plan uses (never lower it).
+    const int lim_col = 128 << 10, lim_row = 112 << 10, lim_spread = 212 << 10;
+    if (rows < 1 || smem_col > (size_t)lim_col || smem_row > (size_t)lim_row ||
+        smem_spread > (size_t)lim_spread) {
+        set_error("fused NFFT: shared memory plan exceeds the kernel limits");
+        return NUDIM_EINVAL;
+    }
     std::vector<double> w0, w1;
     fft_twiddles(n0, &w0);
     fft_twiddles(n1, &w1);
     std::vector<T> t0(w0.begin(), w0.end()), t1(w1.begin(), w1.end());
     auto up = [&](void **dst, const void *srcp, size_t nb) -> int {
-        NUDIM_CUDA(cudaMalloc(dst, nb ? nb : 8));
-        if (nb) NUDIM_CUDA(cudaMemcpy(*dst, srcp, nb, cudaMemcpyHostToDevice));
         bytes += nb;
-        return NUDIM_OK;
+        return upload_async(dst, srcp, nb, st);
     };
     NUDIM_TRY(up((void **)&tw0, t0.data(), sizeof(T) * t0.size()));
     NUDIM_TRY(up((void **)&tw1, t1.data(), sizeof(T) * t1.size()));
     NUDIM_TRY(up((void **)&blk_off, L.blk_off.data(), sizeof(int) * L.blk_off.size()));
     NUDIM_TRY(up((void **)&ent, L.ent.data(), sizeof(int) * L.ent.size()));
     NUDIM_TRY(up((void **)&nslots, L.nslots.data(), L.nslots.size()));
-    NUDIM_TRY(up((void **)&band_row, L.band_row.data(), sizeof(int) * L.band_row.size()));
     NUDIM_TRY(up((void **)&band_off, L.band_off.data(), sizeof(int) * L.band_off.size()));
-    NUDIM_TRY(up((void **)&band_node, L.band_node.data(), sizeof(int) * L.band_node.size()));
-    NUDIM_CUDA(cudaDeviceSynchronize());
-    size_t smem_col = 2 * sizeof(C) * (size_t)BC * n0;
-    size_t smem_row = 2 * sizeof(C) * (size_t)rows * n1;
-    if (smem_col > (227u << 10) || smem_row > (227u << 10) || rows < 1) {
-        set_error("fused NFFT: shared memory plan too large");
-        return NUDIM_EINVAL;
+    NUDIM_TRY(up((void **)&band_node, L.band_node.data(),
+                 sizeof(int) * std::max<size_t>(1, L.band_node.size())));
+    NUDIM_TRY(up((void **)&band_ord, L.band_ord.data(), sizeof(int) * L.band_ord.size()));
+    {
+        std::vector<T> bw(L.band_w.begin(), L.band_w.end());
+        if (bw.empty()) bw.assign(Wa, T(0));
+        NUDIM_TRY(up((void **)&band_w, bw.data(), sizeof(T) * bw.size()));
     }
     NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem_col));
-    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, true>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
-    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, false>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
+                                    lim_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, true, 1>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, false, 1>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, true, 2>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, false, 2>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, true, 4>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, false, 4>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft<T, PM_COMPLEX>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_row));
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft<T, PM_REAL_INIT>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_row));
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop<T, CM_PLAIN>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_row));
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop<T, CM_DOT>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_row));
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop<T, CM_INIT>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_row));
     fused = true;
     return NUDIM_OK;
 }
 
 template <typename T> void NfftDev<T>::release_fused()
 {
-    cudaFree(tw0);
-    cudaFree(tw1);
-    cudaFree(blk_off);
-    cudaFree(ent);
-    cudaFree(nslots);
-    cudaFree(band_row);
-    cudaFree(band_off);
-    cudaFree(band_node);
+    void *ptrs[] = {tw0, tw1, blk_off, ent, nslots, band_off, band_node, band_ord, band_w};
+    for (void *q : ptrs)
+        if (q) cudaFreeAsync(q, ast);
     tw0 = tw1 = nullptr;
-    blk_off = ent = band_row = band_off = band_node = nullptr;
+    blk_off = ent = band_off = band_node = band_ord = nullptr;
+    band_w = nullptr;
     nslots = nullptr;
     fused = false;
 }
@@ -478,11 +599,9 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
     int chunk = fused_chunk(nplanes);
     void *wsv;
     size_t nH = (size_t)N0 * n1 * chunk, nP = (size_t)smax * M * chunk;
-    NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (nH + nP), &wsv));
+    NUDIM_TRY(workspace(sizeof(C) * (nH + nP), &wsv));
     C *H = (C *)wsv, *P = H + nH;
     int logn0 = ilog2(n0), logn1 = ilog2(n1);
-    size_t smem_col = 2 * sizeof(C) * (size_t)BC * n0;
-    size_t smem_row = 2 * sizeof(C) * (size_t)rows * n1;
     const double c = sizeof(C), tab = (double)M * (8 + 2 * kW * sizeof(T));
     for (int p0 = 0; p0 < nplanes; p0 += chunk) {
         int nb = std::min(chunk, nplanes - p0);
@@ -503,8 +622,8 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
         {
             ProfScope ps(ctx, PK_INTERP, st,
                          tab + nb * c * ((double)N0 * n1 + (double)smax * M));
-            k_colfft_interp<T><<<dim3(nblk, nb), 512, smem_col, st>>>(
-                H, N0, n0, logn0, n1, BC, tw0, u, psi, blk_off, ent, M, smax, P);
+            k_colfft_interp<T><<<dim3(nblk, nb), 32 * col_warps<T>(), smem_col, st>>>(
+                H, N0, n0, logn0, n1, BC, nblk, tw0, u, psi, blk_off, ent, M, smax, P);
             NUDIM_LAUNCH_CHECK();
         }
         {
@@ -531,25 +650,30 @@ int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropAr
     int chunk = fused_chunk(nplanes);
     void *wsv;
     size_t nH = (size_t)N0 * n1 * chunk;
-    NUDIM_TRY(ctx_workspace(ctx, sizeof(C) * (nH + (size_t)smax * M * chunk), &wsv));
+    NUDIM_TRY(workspace(sizeof(C) * (nH + (size_t)smax * M * chunk), &wsv));
     C *Hp = (C *)wsv;
     int logn0 = ilog2(n0), logn1 = ilog2(n1);
-    size_t smem_col = 2 * sizeof(C) * (size_t)BC * n0;
-    size_t smem_row = 2 * sizeof(C) * (size_t)rows * n1;
     const double c = sizeof(C), tab = (double)M * (8 + 2 * kW * sizeof(T));
     for (int p0 = 0; p0 < nplanes; p0 += chunk) {
         int nb = std::min(chunk, nplanes - p0);
         {
             ProfScope ps(ctx, PK_SPREAD, st, tab + nb * c * ((double)M + (double)N0 * n1));
-            dim3 g(nblk, nb);
-            if (sa.w)
-                k_spread_colifft<T, true><<<g, 32 * kFusedWarps, smem_col, st>>>(
-                    sa, u, psi, band_row, band_off, band_node, kFusedWarps, N0, n0, logn0, n1, BC,
-                    tw0, p0, Hp);
-            else
-                k_spread_colifft<T, false><<<g, 32 * kFusedWarps, smem_col, st>>>(
-                    sa, u, psi, band_row, band_off, band_node, kFusedWarps, N0, n0, logn0, n1, BC,
-                    tw0, p0, Hp);
+            dim3 g(nblka, ceil_div(nb, Pa));
+            const int thr = 32 * kSpreadWarps;
+#define NUDIM_SPREAD(W, PP)                                                                     \
+    k_spread_colifft<T, W, PP><<<g, thr, smem_spread, st>>>(sa, band_off, band_ord, band_node,  \
+                                                            band_w, nbands, N0, n0, logn0, n1,  \
+                                                            BCa, nb, tw0, p0, Hp)
+            if (sa.w) {
+                if (Pa == 4) NUDIM_SPREAD(true, 4);
+                else if (Pa == 2) NUDIM_SPREAD(true, 2);
+                else NUDIM_SPREAD(true, 1);
+            } else {
+                if (Pa == 4) NUDIM_SPREAD(false, 4);
+                else if (Pa == 2) NUDIM_SPREAD(false, 2);
+                else NUDIM_SPREAD(false, 1);
+            }
+#undef NUDIM_SPREAD
             NUDIM_LAUNCH_CHECK();
         }
         {
@@ -566,8 +690,8 @@ int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropAr
     return NUDIM_OK;
 }
 
-template int NfftDev<double>::init_fused(const NfftTables &);
-template int NfftDev<float>::init_fused(const NfftTables &);
+template int NfftDev<double>::init_fused(const NfftTables &, cudaStream_t);
+template int NfftDev<float>::init_fused(const NfftTables &, cudaStream_t);
 template void NfftDev<double>::release_fused();
 template void NfftDev<float>::release_fused();
 template int NfftDev<double>::fused_chunk(int) const;

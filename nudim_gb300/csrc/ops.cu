@@ -193,12 +193,25 @@ template <typename T> int launch_unpack(const cplx_t<T> *data, T *img, int nz, s
 // reconstruction.c:672-700 / reconstruction-parallel.c:805-833.
 // Inside the support u >= 0 is kept; u < 0 inside, and everything outside,
 // becomes (HIO) img_last - 0.9 u or (ER) 0.  The result replaces img_last.
+// The outer-iteration index lives on the device (set before each iteration)
+// so that one captured graph serves every iteration.
+__global__ void k_set_counter(int *it, int v) { *it = v; }
+
+int launch_set_counter(int *it, int v, cudaStream_t st)
+{
+    k_set_counter<<<1, 1, 0, st>>>(it, v);
+    NUDIM_LAUNCH_CHECK();
+    return NUDIM_OK;
+}
+
 template <typename T>
 __global__ void k_constraint(const T *__restrict__ img, T *__restrict__ last, int np, int nx,
-                             size_t P2, size_t V, int hio, int height, int ylo, int yhi)
+                             size_t P2, size_t V, const int *__restrict__ it, int nhio,
+                             int height, int ylo, int yhi)
 {
     size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= V) return;
+    int hio = *it < nhio;
     size_t i = o % P2;
     int yi = (int)(i / np), xi = (int)(i % np);
     bool inside;
@@ -214,14 +227,14 @@ __global__ void k_constraint(const T *__restrict__ img, T *__restrict__ last, in
 }
 
 template <typename T>
-int launch_constraint(T *img, const T *img_last, int nz, int np, int nx, int hio, int height,
-                      int ylo, int yhi, cudaStream_t st)
+int launch_constraint(T *img, const T *img_last, int nz, int np, int nx, const int *it,
+                      int nhio, int height, int ylo, int yhi, cudaStream_t st)
 {
     // img_last is overwritten with the constrained volume (it becomes the
     // next iteration's img and img_last).
     size_t P2 = (size_t)np * np, V = P2 * nz;
     k_constraint<T><<<ceil_div((long)V, 256), 256, 0, st>>>(img, (T *)img_last, np, nx, P2, V,
-                                                            hio, height, ylo, yhi);
+                                                            it, nhio, height, ylo, yhi);
     NUDIM_LAUNCH_CHECK();
     return NUDIM_OK;
 }
@@ -229,8 +242,9 @@ int launch_constraint(T *img, const T *img_last, int nz, int np, int nx, int hio
 // R-factor of iteration nn: sqrt(sum diff1 / sum diff2) over planes
 // (reconstruction.c:603-604), summed in plane order.
 __global__ void k_finish_r(const double *__restrict__ d12, int nplanes, double *__restrict__ rh,
-                           int nn)
+                           const int *__restrict__ it)
 {
+    int nn = *it;
     __shared__ double sh[32];
     double a = 0, c = 0;
     for (int p = threadIdx.x; p < nplanes; p += blockDim.x) {
@@ -243,14 +257,14 @@ __global__ void k_finish_r(const double *__restrict__ d12, int nplanes, double *
 }
 
 template <typename T>
-int launch_finish_r(const double *part, int nparts, int nplanes, int stride, double *rh, int nn,
-                    cudaStream_t st)
+int launch_finish_r(const double *part, int nparts, int nplanes, int stride, double *rh,
+                    const int *it, cudaStream_t st)
 {
     // part holds per plane [nparts diff1 partials][nparts diff2 partials];
     // reduce them into d12 (stored after the partial area) then across planes.
     double *d12 = (double *)part + (size_t)nplanes * stride;
     launch_finish_sums(part, nparts, nplanes, stride, d12, 2, 2, st);
-    k_finish_r<<<1, 256, 0, st>>>(d12, nplanes, rh, nn);
+    k_finish_r<<<1, 256, 0, st>>>(d12, nplanes, rh, it);
     NUDIM_LAUNCH_CHECK();
     return NUDIM_OK;
 }
@@ -286,9 +300,10 @@ template <typename T> int launch_to_double(const T *src, double *dst, size_t n, 
 #define NUDIM_INST(T)                                                                          \
     template int launch_pack<T>(const T *, cplx_t<T> *, int, size_t, cudaStream_t);           \
     template int launch_unpack<T>(const cplx_t<T> *, T *, int, size_t, cudaStream_t);         \
-    template int launch_constraint<T>(T *, const T *, int, int, int, int, int, int, int,      \
-                                      cudaStream_t);                                          \
-    template int launch_finish_r<T>(const double *, int, int, int, double *, int, cudaStream_t); \
+    template int launch_constraint<T>(T *, const T *, int, int, int, const int *, int, int,   \
+                                      int, int, cudaStream_t);                                \
+    template int launch_finish_r<T>(const double *, int, int, int, double *, const int *,     \
+                                    cudaStream_t);                                            \
     template int launch_real_to<T>(const double *, T *, size_t, cudaStream_t);               \
     template int launch_to_double<T>(const T *, double *, size_t, cudaStream_t);
 NUDIM_INST(double)

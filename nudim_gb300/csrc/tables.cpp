@@ -230,25 +230,33 @@ void fft_twiddles(int n, std::vector<double> *tw)
     }
 }
 
-int build_fused_lists(const NfftTables &t, int BC, int W, FusedLists *L)
+int build_fused_lists(const NfftTables &t, int BC, int BCa, FusedLists *L)
 {
     const int kWin = 2 * 6 + 2;
-    if (BC <= 0 || t.n1 % BC || W <= 0) return -1;
+    if (BC <= 0 || t.n1 % BC) return -1;
+    if (BCa <= 0 || BCa > 32 || 32 % BCa || t.n1 % BCa) return -1;
     int n0 = t.n0, n1 = t.n1, M = t.M;
+    int R = 32 / BCa;
+    if (n0 % R) return -1;
     L->BC = BC;
-    L->W = W;
+    L->BCa = BCa;
+    L->R = R;
     L->nblk = n1 / BC;
-    int nblk = L->nblk;
+    L->nblka = n1 / BCa;
+    L->nbands = n0 / R;
+    int nblk = L->nblk, nb = L->nbands;
     // ---- trafo lists: blocks met by each node's 14 window columns
     std::vector<std::vector<int>> per(nblk);
     L->nslots.assign(M, 0);
     L->smax = 0;
+    // a window may not meet the same block twice (possible only when
+    // n1 < 13 + BC): the column pass sums a node's whole block at once
+    if (n1 < kWin - 1 + BC && nblk > 1) return -2;
     for (int j = 0; j < M; j++) {
-        int first = -1, slot = 0, last = -1;
+        int slot = 0, last = -1;
         for (int s = 0; s < kWin; s++) {
             int b = ((t.u1[j] + s) & (n1 - 1)) / BC;
             if (b == last) continue;
-            if (first < 0) first = b;
             per[b].push_back(j * 8 + slot);
             slot++;
             last = b;
@@ -257,60 +265,106 @@ int build_fused_lists(const NfftTables &t, int BC, int W, FusedLists *L)
         if (slot > L->smax) L->smax = slot;
     }
     if (L->smax > 8) return -1;
+    // Entry order inside a block (one column-pass lane per entry): entries
+    // with equal numbers of window columns inside the block side by side
+    // (longest first), so a warp's lanes run equal loops; inside such a run
+    // the first window rows u0 cycle through the 16 residues mod 16, so the
+    // 32 lanes of a warp read shared-memory rows spread over all banks.
+    for (int b = 0; b < nblk; b++) {
+        auto cols = [&](int en) {
+            int j = en / 8, k = 0;
+            for (int s = 0; s < kWin; s++) k += ((t.u1[j] + s) & (n1 - 1)) / BC == b;
+            return k;
+        };
+        std::vector<std::pair<int, int>> key(per[b].size());
+        for (size_t i = 0; i < key.size(); i++) key[i] = {-cols(per[b][i]), per[b][i]};
+        std::sort(key.begin(), key.end());
+        std::vector<int> out;
+        out.reserve(key.size());
+        for (size_t i = 0; i < key.size();) {
+            size_t k = i;
+            while (k < key.size() && key[k].first == key[i].first) k++;
+            std::vector<int> bucket[16];
+            for (size_t q = i; q < k; q++)
+                bucket[t.u0[key[q].second / 8] & 15].push_back(key[q].second);
+            size_t head[16] = {0};
+            for (size_t left = k - i; left > 0;)
+                for (int r = 0; r < 16; r++)
+                    if (head[r] < bucket[r].size()) {
+                        out.push_back(bucket[r][head[r]++]);
+                        left--;
+                    }
+            i = k;
+        }
+        per[b] = out;
+    }
     L->blk_off.assign(nblk + 1, 0);
     for (int b = 0; b < nblk; b++) L->blk_off[b + 1] = L->blk_off[b] + (int)per[b].size();
     L->ent.clear();
     L->ent.reserve(L->blk_off[nblk]);
     for (int b = 0; b < nblk; b++) L->ent.insert(L->ent.end(), per[b].begin(), per[b].end());
-    // ---- adjoint lists: per block, W bands of rows with balanced work
-    L->band_row.assign((size_t)nblk * (W + 1), 0);
-    L->band_off.assign((size_t)nblk * W + 1, 0);
-    L->band_node.clear();
-    std::vector<double> load(n0);
-    std::vector<std::vector<int>> bandlist(W);
-    for (int b = 0; b < nblk; b++) {
-        std::fill(load.begin(), load.end(), 0.0);
-        for (int e = L->blk_off[b]; e < L->blk_off[b + 1]; e++) {
-            int j = L->ent[e] / 8;
-            int cols = 0;
-            for (int s = 0; s < kWin; s++) cols += (((t.u1[j] + s) & (n1 - 1)) / BC) == b;
-            for (int s = 0; s < kWin; s++) load[(t.u0[j] + s) & (n0 - 1)] += cols + 2.0;
-        }
-        double tot = 0;
-        for (int r = 0; r < n0; r++) tot += load[r] + 1e-3;
-        int *br = &L->band_row[(size_t)b * (W + 1)];
-        br[0] = 0;
-        double acc = 0;
-        int w = 1;
-        for (int r = 0; r < n0 && w < W; r++) {
-            acc += load[r] + 1e-3;
-            while (w < W && acc >= tot * w / W) br[w++] = r + 1;
-        }
-        while (w < W) br[w++] = n0;
-        br[W] = n0;
-        for (int v = 0; v < W; v++) bandlist[v].clear();
-        for (int e = L->blk_off[b]; e < L->blk_off[b + 1]; e++) {
-            int j = L->ent[e] / 8;
-            int lastv = -1;
-            // window rows are 14 consecutive rows modulo n0; bands are
-            // contiguous row ranges, so collect each band once
-            bool hit[64] = {false};
-            for (int s = 0; s < kWin; s++) {
-                int r = (t.u0[j] + s) & (n0 - 1);
-                int v = 0;
-                while (v + 1 < W && r >= br[v + 1]) v++;
-                if (v != lastv && !hit[v]) {
-                    bandlist[v].push_back(j);
-                    hit[v] = true;
-                }
-                lastv = v;
+    // ---- adjoint lists: tiles of R x BCa grid points (one per warp lane);
+    // per tile the nodes whose window meets it, ascending.  Tiles are
+    // numbered block-major: tile = b * nbands + v.
+    const int nblka = L->nblka;
+    std::vector<int> bstamp(nblka, -1), vstamp(nb, -1);
+    int blks[16], bands[16];
+    auto visit = [&](int j, auto &&fn) {
+        int nbk = 0, nbd = 0;
+        for (int s = 0; s < kWin; s++) {
+            int b = ((t.u1[j] + s) & (n1 - 1)) / BCa;
+            int v = ((t.u0[j] + s) & (n0 - 1)) / R;
+            if (bstamp[b] != j) {
+                bstamp[b] = j;
+                blks[nbk++] = b;
+            }
+            if (vstamp[v] != j) {
+                vstamp[v] = j;
+                bands[nbd++] = v;
             }
         }
-        for (int v = 0; v < W; v++) {
-            std::sort(bandlist[v].begin(), bandlist[v].end());
-            L->band_node.insert(L->band_node.end(), bandlist[v].begin(), bandlist[v].end());
-            L->band_off[(size_t)b * W + v + 1] = (int)L->band_node.size();
-        }
+        for (int a = 0; a < nbk; a++)
+            for (int c = 0; c < nbd; c++) fn((size_t)blks[a] * nb + bands[c]);
+    };
+    size_t ntiles = (size_t)nblka * nb;
+    std::vector<int> cnt(ntiles + 1, 0);
+    for (int j = 0; j < M; j++) visit(j, [&](size_t tile) { cnt[tile + 1]++; });
+    for (size_t i = 0; i < ntiles; i++) cnt[i + 1] += cnt[i];
+    L->band_off = cnt;
+    L->band_node.assign(cnt[ntiles], 0);
+    // per entry the tile's window weights: R row weights psi0(v*R + rr - u0)
+    // then BCa column weights psi1(b*BCa + cc - u1), zero outside the window
+    const int W = R + BCa;
+    L->band_w.assign((size_t)cnt[ntiles] * W, 0.0);
+    std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+    std::fill(bstamp.begin(), bstamp.end(), -1);
+    std::fill(vstamp.begin(), vstamp.end(), -1);
+    for (int j = 0; j < M; j++)
+        visit(j, [&](size_t tile) {
+            int e = pos[tile]++;
+            L->band_node[e] = j;
+            int b = (int)(tile / nb), v = (int)(tile % nb);
+            double *w = &L->band_w[(size_t)e * W];
+            const double *ps = &t.psi[(size_t)j * 2 * kWin];
+            for (int rr = 0; rr < R; rr++) {
+                int d = (v * R + rr - t.u0[j]) & (n0 - 1);
+                if (d < kWin) w[rr] = ps[d];
+            }
+            for (int cc = 0; cc < BCa; cc++) {
+                int d = (b * BCa + cc - t.u1[j]) & (n1 - 1);
+                if (d < kWin) w[R + cc] = ps[kWin + d];
+            }
+        });
+    // per block, its tiles longest list first (the spreading CTA hands
+    // them out in this order)
+    L->band_ord.resize(ntiles);
+    for (int b = 0; b < nblka; b++) {
+        int *o = &L->band_ord[(size_t)b * nb];
+        for (int v = 0; v < nb; v++) o[v] = v;
+        const int *c = &cnt[(size_t)b * nb];
+        std::stable_sort(o, o + nb, [&](int x, int y) {
+            return c[x + 1] - c[x] > c[y + 1] - c[y];
+        });
     }
     return 0;
 }

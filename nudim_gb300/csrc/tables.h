@@ -39,17 +39,23 @@ int build_nfft_tables(int N0, int N1, int M, const double *x, int ty, int tx, Nf
 // oversampled grid):
 //   trafo:   per block, the nodes whose window columns meet the block, each
 //            with its partial slot (0 = the node's first block, 1, ...);
-//   adjoint: per block, W row bands balanced by window-cell count, and per
-//            (block, band) the nodes whose window meets that band.
+//   adjoint: column blocks of BCa columns; per tile of R = 32 / BCa rows x
+//            BCa columns (one grid point per warp lane), the nodes whose
+//            window meets the tile, ascending.
 struct FusedLists {
-    int BC = 0, nblk = 0, W = 0, smax = 0;
+    int BC = 0, nblk = 0, smax = 0;
+    int BCa = 0, nblka = 0, R = 0, nbands = 0;
     std::vector<int> blk_off, ent;          // ent = node * 8 + slot
     std::vector<unsigned char> nslots;      // blocks per node
-    std::vector<int> band_row;              // nblk * (W + 1) row boundaries
-    std::vector<int> band_off, band_node;   // CSR over (block, band)
+    std::vector<int> band_off, band_node;   // CSR over tiles b * nbands + v
+    std::vector<double> band_w;             // per entry R row + BCa column weights
+    std::vector<int> band_ord;              // per block its tiles, longest list first
 };
 
-int build_fused_lists(const NfftTables &t, int BC, int W, FusedLists *L);
+// BC a power of two dividing n1; BCa a power of two <= 32 dividing n1.
+// Returns 0, -1 (bad shape) or -2 (a window meets one trafo block twice:
+// the grid is too narrow for column blocks of BC).
+int build_fused_lists(const NfftTables &t, int BC, int BCa, FusedLists *L);
 
 // e^{-2 pi i k / n}, k < n, interleaved (re, im)
 void fft_twiddles(int n, std::vector<double> *tw);

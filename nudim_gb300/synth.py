@@ -31,6 +31,8 @@ def blob_phantom(shape, nblobs, radius, sigma_range, amp_range, seed, nshells=0)
         zs = slice(max(0, int(z0) - h), min(nz, int(z0) + h + 2))
         ys = slice(max(0, int(y0) - h), min(ny, int(y0) + h + 2))
         xs = slice(max(0, int(x0) - h), min(nx, int(x0) + h + 2))
+        if zs.stop <= zs.start or ys.stop <= ys.start or xs.stop <= xs.start:
+            continue  # blob entirely outside a thin volume
         z = np.arange(zs.start, zs.stop)[:, None, None] - z0
         y = np.arange(ys.start, ys.stop)[None, :, None] - y0
         x = np.arange(xs.start, xs.stop)[None, None, :] - x0
