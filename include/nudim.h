@@ -236,6 +236,22 @@ int nudim_cgnr(nudim_nfft_plan *plan, int nplanes, const void *y, const void *w,
 int nudim_tv(nudim_ctx *ctx, int precision, void *vol, int nz, int ny, int nx, float lam,
              int niter, int height, int nheight, int ncenter, void *stream);
 
+/* nudim_tv without any device allocation.  No counterpart in the reference:
+ * it serves callers that cannot call cudaMalloc (a host whose memory
+ * manager owns the whole device, or a loop that must avoid the implicit
+ * synchronisation of cudaMalloc/cudaFree).  Same semantics and kernels as
+ * nudim_tv on the current CUDA device; the scratch (gradient field and sums)
+ * is one fixed 32 MiB device array inside this library, present on every
+ * GPU that loads it until the process exits: a volume needs
+ * 8*(2*ceil(nz*ny*nx/256)+6) bytes (rounded up to 256) plus one real per
+ * voxel, so FP64 volumes up to about 4.1 million voxels (FP32 about 8.2
+ * million) fit; larger ones return NUDIM_EINVAL.  The first call on a device
+ * looks up the array's device address; make that first call before any
+ * stream capture.  All calls share the array: calls whose work overlaps on a
+ * GPU race and must be serialised by the caller. */
+int nudim_tv_noalloc(int precision, void *vol, int nz, int ny, int nx, float lam, int niter,
+                     int height, int nheight, int ncenter, void *stream);
+
 /* aniso_diffusion_2d (denoise.c:320-378), in place, Gauss-Seidel order per
  * Z-plane.  nx_bound is the value the reference compares the column index
  * with (its "nx" argument, the number of Z-planes in reconstruction.c:627);

@@ -58,6 +58,7 @@ EXPORTS = [
     ("nudim_nfft_adjoint", _ip, [_vp, _ip, _vp, _vp, _vp]),
     ("nudim_cgnr", _ip, [_vp, _ip, _vp, _vp, _vp, _ip, _vp]),
     ("nudim_tv", _ip, [_vp, _ip, _vp, _ip, _ip, _ip, C.c_float, _ip, _ip, _ip, _ip, _vp]),
+    ("nudim_tv_noalloc", _ip, [_ip, _vp, _ip, _ip, _ip, C.c_float, _ip, _ip, _ip, _ip, _vp]),
     ("nudim_diffusion2d", _ip, [_vp, _ip, _vp, _ip, _ip, _ip, _ip, C.c_float, C.c_float, _ip,
                                 _vp]),
 ]
@@ -339,6 +340,14 @@ def tv(ctx, vol_ptr, shape, precision=FP64, lam=0.2, niter=40, height=0, nheight
     nz, ny, nx = shape
     _check(lib().nudim_tv(ctx.h, precision, vol_ptr, nz, ny, nx, lam, niter, height, nheight,
                           ncenter, stream))
+
+
+def tv_noalloc(vol_ptr, shape, precision=FP64, lam=0.2, niter=40, height=0, nheight=0,
+               ncenter=0, stream=None):
+    """nudim_tv for callers that cannot allocate device memory (fixed scratch)."""
+    nz, ny, nx = shape
+    _check(lib().nudim_tv_noalloc(precision, vol_ptr, nz, ny, nx, lam, niter, height, nheight,
+                                  ncenter, stream))
 
 
 def diffusion2d(ctx, vol_ptr, shape, nx_bound, precision=FP64, lam=0.25, kappa=0.005,
