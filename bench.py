@@ -194,6 +194,16 @@ def timed_steps(ctx, job, steps, nvtx=None):
     return e0.elapsed_time(e1)
 
 
+# DRAM traffic over algorithmic bytes of one launch, from one ncu capture of a
+# 20-plane launch of the same kernel on the same geometry (profiles/*_cfg2_20planes.md):
+# dram__bytes_read.sum + dram__bytes_write.sum divided by the profiler's algorithmic
+# bytes for that launch.  Traffic grows in proportion to the planes of a launch.
+MEASURED_TRAFFIC_RATIO = {
+    "spread": (58.727936e6 + 34.508544e6) / (69504 * 120 + 20 * 8 * (69504 + 384 * 1024)),
+    "interp": (84.525312e6 + 14.749440e6) / (69504 * 120 + 20 * 8 * (384 * 1024 + 3 * 69504)),
+}
+
+
 def roofline_from_profile(prof, peak_gbs, peak_kind):
     mine = {k: v for k, v in prof.items() if k not in ("fft2d", "zfft") and v[1] > 0}
     total = sum(v[0] for v in prof.values())
@@ -202,9 +212,11 @@ def roofline_from_profile(prof, peak_gbs, peak_kind):
     per_launch_s = ms / n / 1e3
     achieved = (b / n) / per_launch_s / 1e9
     shares = {k: round(v[0] / total, 4) for k, v in prof.items() if v[1] > 0}
+    ratio = MEASURED_TRAFFIC_RATIO.get(top)
     return top, {
         "bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak_gbs,
-        "unit": "GB/s", "frac": round(achieved / peak_gbs, 4), "traffic": None,
+        "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
+        "traffic": round(ratio * b / n) if ratio else None,
         "algorithmic_bytes_per_launch": b / n, "avg_launch_ms": ms / n,
         "peak_source": peak_kind}, shares
 

@@ -114,6 +114,24 @@ __device__ __forceinline__ double block_sum(double v, double *sh /* >= 32 */)
     return v;
 }
 
+// Block sum of per-thread values of type T.  FP32: the warps reduce in FP32
+// and only the per-warp partials are summed in FP64 (FP64 arithmetic is
+// slow on this GPU); FP64: block_sum.  Result valid in thread 0.
+template <typename T> __device__ __forceinline__ double block_sum_t(T v, double *sh)
+{
+    if (sizeof(T) == 8) return block_sum((double)v, sh);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) sh[wid] = (double)v;
+    __syncthreads();
+    int nw = (blockDim.x + 31) >> 5;
+    double d = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+    if (wid == 0) d = warp_sum(d);
+    return d;
+}
+
 // Sum `nparts` per-block partials of each of `nplanes` planes, for each of
 // `nsums` sums laid out back to back inside a plane's slot:
 //   out[p*out_stride + k] = sum_i part[p*stride_in + k*nparts + i]

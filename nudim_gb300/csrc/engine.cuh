@@ -166,6 +166,9 @@ template <typename T> struct NfftDev {
     int *blk_off = nullptr, *ent = nullptr, *band_off = nullptr, *band_node = nullptr,
         *band_ord = nullptr;
     T *band_w = nullptr;            // per adjoint tile entry: R row + BCa column weights
+    int nE = 0;                     // trafo entries; their records (structure of arrays):
+    int *e_rb = nullptr, *e_cc = nullptr;
+    T *e_qa = nullptr, *e_q1 = nullptr;
     unsigned char *nslots = nullptr;
 
     // uploads go on stream st (tables are consumed by later work on st)

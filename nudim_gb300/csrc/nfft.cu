@@ -308,7 +308,7 @@ k_interp(const cplx_t<T> *__restrict__ grid, int n0, int n1, const int2 *__restr
     int b = blockIdx.y, gb = plane0 + b;
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     const C *g = grid + (size_t)b * n0 * n1;
-    double s0 = 0, s1 = 0;
+    T s0 = 0, s1 = 0;
     if (j < M) {
         int2 uu = u[j];
         const T *ps = psi + (size_t)j * 2 * kW;
@@ -338,25 +338,25 @@ k_interp(const cplx_t<T> *__restrict__ grid, int n0, int n1, const int2 *__restr
             a.out[o] = mkc<T>(yv.x - f.x, yv.y - f.y);
         } else if (MODE == IM_DOTV) {
             a.out[o] = f;
-            double wv = a.w ? (double)a.w[j] : 1.0;
-            s0 = wv * ((double)f.x * f.x + (double)f.y * f.y);
+            T wv = a.w ? a.w[j] : T(1);
+            s0 = wv * (f.x * f.x + f.y * f.y);
         } else {  // IM_CONSTRAINT: y = known ? s : f, R-factor partials
             if (a.known[j / a.line_len]) {
                 C sv = a.s[(size_t)gb * a.s_stride + j];
                 a.out[o] = sv;
                 T dr = f.x - sv.x, di = f.y - sv.y, pr = f.x + sv.x, pi = f.y + sv.y;
-                s0 = (double)dr * dr + (double)di * di;
-                s1 = (double)pr * pr + (double)pi * pi;
+                s0 = dr * dr + di * di;
+                s1 = pr * pr + pi * pi;
             } else {
                 a.out[o] = f;
             }
         }
     }
     if (MODE == IM_DOTV || MODE == IM_CONSTRAINT) {
-        double v0 = block_sum(s0, sh);
+        double v0 = block_sum_t<T>(s0, sh);
         if (threadIdx.x == 0) a.part[(size_t)gb * a.part_stride + blockIdx.x] = v0;
         if (MODE == IM_CONSTRAINT) {
-            double v1 = block_sum(s1, sh);
+            double v1 = block_sum_t<T>(s1, sh);
             if (threadIdx.x == 0)
                 a.part[(size_t)gb * a.part_stride + gridDim.x + blockIdx.x] = v1;
         }
@@ -437,7 +437,7 @@ k_crop(const cplx_t<T> *__restrict__ grid, int n0, int n1, int N0, int N1,
     int b = blockIdx.y, gb = plane0 + b;
     size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t NN = (size_t)N0 * N1;
-    double s = 0;
+    T s = 0;
     if (k < NN) {
         int ai = (int)(k / N1), ci = (int)(k % N1);
         int l0 = (ai - N0 / 2) & (n0 - 1), l1 = (ci - N1 / 2) & (n1 - 1);
@@ -446,11 +446,11 @@ k_crop(const cplx_t<T> *__restrict__ grid, int n0, int n1, int N0, int N1,
         C z = mkc<T>(g.x * sc, g.y * sc);
         a.out[(size_t)gb * a.out_stride + k] = z;
         if (MODE == CM_INIT) a.p_out[(size_t)gb * a.out_stride + k] = z;
-        s = (double)z.x * z.x + (double)z.y * z.y;
+        s = z.x * z.x + z.y * z.y;
     }
     if (MODE != CM_PLAIN) {
-        s = block_sum(s, sh);
-        if (threadIdx.x == 0) a.part[(size_t)gb * a.part_stride + blockIdx.x] = s;
+        double d = block_sum_t<T>(s, sh);
+        if (threadIdx.x == 0) a.part[(size_t)gb * a.part_stride + blockIdx.x] = d;
     }
 }
 

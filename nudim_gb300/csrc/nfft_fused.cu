@@ -147,15 +147,20 @@ template <typename T> __host__ __device__ constexpr int col_warps() { return siz
 // Shared memory: two BC x n0 complex buffers (FFT).  After the column FFTs
 // each lane takes one (node, block) entry of the block's list and sums the
 // node's window over the block's columns: for each of the cnt columns
-// inside the window, the 14-row column sum weighted by psi0, then weighted
-// by the column's psi1.  The list holds entries with equal cnt side by side,
-// so the lanes of a warp run loops of equal length.
+// inside the window, the 14-row column sum weighted by the row weights,
+// then weighted by the column's weight.  Entry records are structures of
+// arrays (coalesced across the lanes); rows are read in 16-byte aligned
+// pairs (FP32) against 16 row weights pre-shifted to the even first row.
+// The list holds entries with equal cnt side by side, so the lanes of a
+// warp run loops of equal length.
 template <typename T>
 __global__ void __launch_bounds__(32 * col_warps<T>(), 1)
 k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int n1, int BC,
-                int nblk, const cplx_t<T> *__restrict__ tw0, const int2 *__restrict__ u,
-                const T *__restrict__ psi, const int *__restrict__ blk_off,
-                const int *__restrict__ ent, int M, int smax, cplx_t<T> *__restrict__ part)
+                const cplx_t<T> *__restrict__ tw0, const int *__restrict__ blk_off,
+                const int *__restrict__ ent, const int *__restrict__ e_rb,
+                const int *__restrict__ e_cc, const T *__restrict__ e_qa,
+                const T *__restrict__ e_q1, int nE, int M, int smax,
+                cplx_t<T> *__restrict__ part)
 {
     using C = cplx_t<T>;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -174,47 +179,39 @@ k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int 
     __syncthreads();
     const C *G = block_fft<T, -1>(A, B, n0, logn0, BC, tw0);
     const int beg = blk_off[cb], end = blk_off[cb + 1];
-    const int col0 = cb * BC, m0 = n0 - 1;
+    const int m0 = n0 - 1;
     for (int e = beg + threadIdx.x; e < end; e += blockDim.x) {
-        const int en = ent[e], j = en >> 3;
-        const int2 uu = u[j];
-        const T *ps = psi + (size_t)j * 2 * kW;
-        // the row weights as 16-byte vectors (a psi row is 2 kW = 28
-        // values: 112 or 224 bytes, so every row starts 16-byte aligned)
-        using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
-        constexpr int TV = sizeof(V) / sizeof(T), NV = (kW + TV - 1) / TV;
-        T q0[NV * TV];
+        const int js = ent[e], rb = e_rb[e], ccn = e_cc[e];
+        const int cl0 = ccn & 255, cnt = ccn >> 8;
+        T qa[16];
 #pragma unroll
-        for (int i = 0; i < NV; i++) {
-            V x = ((const V *)ps)[i];
-            memcpy(&q0[i * TV], &x, sizeof(V));
-        }
-        // the window's columns inside this block: cnt columns from block
-        // column cl0 (window column t1lo); one block: all kW, wrapping
-        int t1lo = 0, cl0 = 0, cnt = kW;
-        if (nblk > 1) {
-            int dd = (col0 - uu.y) & (n1 - 1);
-            if (dd < kW) t1lo = dd;
-            else cl0 = (uu.y - col0) & (n1 - 1);
-            cnt = min(kW - t1lo, BC - cl0);
-        }
+        for (int i = 0; i < 16; i++) qa[i] = e_qa[(size_t)i * nE + e];
         T ar = 0, ai = 0;
         for (int q = 0; q < cnt; q++) {
-            int t1 = t1lo + q;
-            int cl = nblk > 1 ? cl0 + q : ((uu.y + t1) & (n1 - 1));
-            const C *gp = G + (size_t)cl * n0;
+            const C *gp = G + (size_t)((cl0 + q) & (BC - 1)) * n0;
             T sr = 0, si = 0;
+            if (sizeof(T) == 4) {
 #pragma unroll
-            for (int t = 0; t < kW; t++) {
-                C g = gp[(uu.x + t) & m0];
-                sr += q0[t] * g.x;
-                si += q0[t] * g.y;
+                for (int i = 0; i < 8; i++) {
+                    float4 pr = *(const float4 *)(gp + ((rb + 2 * i) & m0));
+                    sr += qa[2 * i] * (T)pr.x;
+                    si += qa[2 * i] * (T)pr.y;
+                    sr += qa[2 * i + 1] * (T)pr.z;
+                    si += qa[2 * i + 1] * (T)pr.w;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    C g = gp[(rb + i) & m0];
+                    sr += qa[i] * g.x;
+                    si += qa[i] * g.y;
+                }
             }
-            T w = ps[kW + t1];
+            T w = e_q1[(size_t)q * nE + e];
             ar += w * sr;
             ai += w * si;
         }
-        part[((size_t)b * smax + (en & 7)) * M + j] = mkc<T>(ar, ai);
+        part[((size_t)b * smax + (js & 7)) * M + (js >> 3)] = mkc<T>(ar, ai);
     }
 }
 
@@ -228,7 +225,7 @@ k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ 
     __shared__ double sh[32];
     int b = blockIdx.y, gb = plane0 + b;
     int j = blockIdx.x * blockDim.x + threadIdx.x;
-    double s0 = 0, s1 = 0;
+    T s0 = 0, s1 = 0;
     if (j < M) {
         int ns = nslots[j];
         C f = part[((size_t)b * smax) * M + j];
@@ -245,25 +242,25 @@ k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ 
             a.out[o] = mkc<T>(yv.x - f.x, yv.y - f.y);
         } else if (MODE == IM_DOTV) {
             a.out[o] = f;
-            double wv = a.w ? (double)a.w[j] : 1.0;
-            s0 = wv * ((double)f.x * f.x + (double)f.y * f.y);
+            T wv = a.w ? a.w[j] : T(1);
+            s0 = wv * (f.x * f.x + f.y * f.y);
         } else {
             if (a.known[j / a.line_len]) {
                 C sv = a.s[(size_t)gb * a.s_stride + j];
                 a.out[o] = sv;
                 T dr = f.x - sv.x, di = f.y - sv.y, pr = f.x + sv.x, pi = f.y + sv.y;
-                s0 = (double)dr * dr + (double)di * di;
-                s1 = (double)pr * pr + (double)pi * pi;
+                s0 = dr * dr + di * di;
+                s1 = pr * pr + pi * pi;
             } else {
                 a.out[o] = f;
             }
         }
     }
     if (MODE == IM_DOTV || MODE == IM_CONSTRAINT) {
-        double v0 = block_sum(s0, sh);
+        double v0 = block_sum_t<T>(s0, sh);
         if (threadIdx.x == 0) a.part[(size_t)gb * a.part_stride + blockIdx.x] = v0;
         if (MODE == IM_CONSTRAINT) {
-            double v1 = block_sum(s1, sh);
+            double v1 = block_sum_t<T>(s1, sh);
             if (threadIdx.x == 0) a.part[(size_t)gb * a.part_stride + gridDim.x + blockIdx.x] = v1;
         }
     }
@@ -277,20 +274,45 @@ k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ 
 // per-point order of the grid path.  Each list entry carries the tile's
 // window weights (R row weights, BC column weights, zero outside the
 // window), so a node costs a lane two weight reads, one product and two
-// FMAs per plane.  FP32: plain sums within a batch of kStage nodes,
-// compensated (Neumaier) sums across batches.  The tile sums go to S_p;
-// then per plane n0-point inverse FFTs of the BC columns.
+// FMAs per plane.  FP32: plain sums within a batch of NB nodes, compensated
+// (Neumaier) sums across batches.  The tile sums go to S_p; then per plane
+// n0-point inverse FFTs of the BC columns.
+//
+// A warp walks its batches (NB list entries; an empty tile is one empty
+// batch) as a two-stage pipeline: while batch i is summed, the weights and
+// node ids of batch i+1 -- the next batch of the tile or the first of the
+// warp's next tile -- arrive by cp.async in the other stage buffer.
 // Shared memory: S_0..S_{P-1}, K (BC x n0 complex each; K is FFT scratch),
-// then the warps' node stages.
+// then the warps' stages.
 constexpr int kSpreadWarps = 16;
 constexpr int kMaxBands = 1024;
 
 template <typename T> __host__ __device__ constexpr int spread_batch() { return sizeof(T) == 4 ? 16 : 8; }
 
-// stage of one warp: weights [NB][W] (W = R + BC = 12 for BC = 4), node values [P][NB]
+// stage of one warp: node values [P][NB], weights [2][NB][W], node ids [2][NB]
 template <typename T, int P> __host__ __device__ constexpr size_t spread_stage_bytes(int W)
 {
-    return (size_t)spread_batch<T>() * (W * sizeof(T) + P * sizeof(cplx_t<T>));
+    return (size_t)spread_batch<T>() * (P * sizeof(cplx_t<T>) + 2 * W * sizeof(T) + 2 * sizeof(int));
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem),
+                 "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem, int src_bytes)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem),
+                 "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 template <typename T, bool WEIGHTED, int P>
@@ -303,6 +325,7 @@ k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
 {
     using C = cplx_t<T>;
     constexpr int NB = spread_batch<T>();
+    constexpr int TV = 16 / sizeof(T);  // weights per 16-byte copy
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ int next_tile, s_off[kMaxBands + 1], s_ord[kMaxBands];
     const size_t buf = (size_t)BC * n0;
@@ -312,8 +335,9 @@ k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     const int R = 32 / BC, W = R + BC;
     unsigned char *wst = (unsigned char *)(K + buf) + warp * spread_stage_bytes<T, P>(W);
-    T *ws = (T *)wst;                  // [NB][W]
-    C *fs = (C *)(ws + NB * W);        // [P][NB]
+    C *fs = (C *)wst;                        // [P][NB]
+    T *ws = (T *)(fs + P * NB);              // [2][NB * W]
+    int *jb = (int *)(ws + 2 * NB * W);      // [2][NB]
     const int rr = lane / BC, cc = lane - rr * BC;
     for (int i = threadIdx.x; i <= nbands; i += blockDim.x) {
         s_off[i] = band_off[(size_t)cb * nbands + i];
@@ -321,90 +345,132 @@ k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
     }
     if (threadIdx.x == 0) next_tile = nwarps;
     __syncthreads();
-    // weights of a batch move as 16-byte vectors
-    using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
-    constexpr int TV = sizeof(V) / sizeof(T);
-    for (int it = warp; it < nbands;) {
-        const int v = s_ord[it];
-        const int r = v * R + rr;
-        const int beg = s_off[v], end = s_off[v + 1];
-        T ar[P], ai[P];
-        Comp<T> kr[P], ki[P];
-#pragma unroll
-        for (int p = 0; p < P; p++) {
-            ar[p] = ai[p] = T(0);
-            kr[p].init();
-            ki[p].init();
-        }
-        for (int base = beg; base < end; base += NB) {
-            const int n = min(NB, end - base);
-            // node values (zero past the list end)
-            if (lane < NB) {
-                int jl = lane < n ? band_node[base + lane] : 0;
-                T wv = (WEIGHTED && lane < n) ? sa.w[jl] : T(1);
-#pragma unroll
-                for (int p = 0; p < P; p++) {
-                    C fv = mkc<T>(0, 0);
-                    if (lane < n && p < np) {
-                        fv = sa.f[(size_t)(plane0 + pb + p) * sa.f_stride + jl];
-                        if (WEIGHTED) fv = mkc<T>(wv * fv.x, wv * fv.y);
-                    }
-                    fs[p * NB + lane] = fv;
-                }
-            }
-            // weights (zero past the list end)
-            const V *src = (const V *)(band_w + (size_t)base * W);
-            for (int q = lane; q < NB * W / TV; q += 32) {
-                V val;
-                if (q * TV < n * W) val = src[q];
-                else memset(&val, 0, sizeof(V));
-                ((V *)ws)[q] = val;
-            }
-            __syncwarp();
-            T br[P], bi[P];
-#pragma unroll
-            for (int p = 0; p < P; p++) br[p] = bi[p] = T(0);
-#pragma unroll
-            for (int k = 0; k < NB; k++) {
-                T q0 = ws[k * W + rr], q1 = ws[k * W + R + cc];
-                if (sizeof(T) == 4) {
-                    T q = q0 * q1;
-#pragma unroll
-                    for (int p = 0; p < P; p++) {
-                        C fv = fs[p * NB + k];
-                        br[p] += q * fv.x;
-                        bi[p] += q * fv.y;
-                    }
-                } else {
-#pragma unroll
-                    for (int p = 0; p < P; p++) {
-                        C fv = fs[p * NB + k];
-                        ar[p] += q1 * (q0 * fv.x);
-                        ai[p] += q1 * (q0 * fv.y);
-                    }
-                }
-            }
-            if (sizeof(T) == 4) {
-#pragma unroll
-                for (int p = 0; p < P; p++) {
-                    kr[p].add(br[p]);
-                    ki[p].add(bi[p]);
-                }
-            }
-            __syncwarp();
-        }
-#pragma unroll
-        for (int p = 0; p < P; p++) {
-            if (sizeof(T) == 4) {
-                ar[p] = kr[p].value();
-                ai[p] = ki[p].value();
-            }
-            S[p * buf + (size_t)cc * n0 + r] = mkc<T>(ar[p], ai[p]);
-        }
+    auto fetch = [&]() {
         int nv = 0;
         if (lane == 0) nv = atomicAdd(&next_tile, 1);
-        it = __shfl_sync(0xffffffffu, nv, 0);
+        return __shfl_sync(0xffffffffu, nv, 0);
+    };
+    // copy batch [base, min(base + NB, end)) of the lists into stage s
+    auto issue = [&](int s, int base, int end) {
+        const int n = min(NB, end - base);
+        T *wd = ws + s * NB * W;
+        const T *wsrc = band_w + (size_t)base * W;
+        for (int q = lane; q < NB * W / TV; q += 32) {
+            bool in = q * TV < n * W;
+            cp_async16(wd + q * TV, in ? (const void *)(wsrc + q * TV) : (const void *)band_w,
+                       in ? 16 : 0);
+        }
+        if (lane < NB) {
+            bool in = lane < n;
+            cp_async4(jb + s * NB + lane, in ? (const void *)(band_node + base + lane)
+                                             : (const void *)band_node,
+                      in ? 4 : 0);
+        }
+    };
+    int it = warp, v = 0, base = 0, end = 0;
+    if (it < nbands) {
+        v = s_ord[it];
+        base = s_off[v];
+        end = s_off[v + 1];
+        issue(0, base, end);
     }
+    cp_async_commit();
+    int it_nx = fetch();
+    int sb = 0;
+    T ar[P], ai[P];
+    Comp<T> kr[P], ki[P];
+#pragma unroll
+    for (int p = 0; p < P; p++) {
+        ar[p] = ai[p] = T(0);
+        kr[p].init();
+        ki[p].init();
+    }
+    while (it < nbands) {
+        // the batch after this one
+        const bool last = base + NB >= end;
+        int nit = it, nv = v, nbase = base + NB, nend = end;
+        if (last) {
+            nit = it_nx;
+            if (nit < nbands) {
+                nv = s_ord[nit];
+                nbase = s_off[nv];
+                nend = s_off[nv + 1];
+            }
+        }
+        if (nit < nbands) issue(sb ^ 1, nbase, nend);
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncwarp();
+        const int n = min(NB, end - base);
+        // node values of this batch (zero past the list end)
+        if (lane < NB) {
+            int jl = jb[sb * NB + lane];
+            T wv = (WEIGHTED && lane < n) ? sa.w[jl] : T(1);
+#pragma unroll
+            for (int p = 0; p < P; p++) {
+                C fv = mkc<T>(0, 0);
+                if (lane < n && p < np) {
+                    fv = sa.f[(size_t)(plane0 + pb + p) * sa.f_stride + jl];
+                    if (WEIGHTED) fv = mkc<T>(wv * fv.x, wv * fv.y);
+                }
+                fs[p * NB + lane] = fv;
+            }
+        }
+        __syncwarp();
+        const T *wc = ws + sb * NB * W;
+        T br[P], bi[P];
+#pragma unroll
+        for (int p = 0; p < P; p++) br[p] = bi[p] = T(0);
+#pragma unroll
+        for (int k = 0; k < NB; k++) {
+            T q0 = wc[k * W + rr], q1 = wc[k * W + R + cc];
+            if (sizeof(T) == 4) {
+                T q = q0 * q1;
+#pragma unroll
+                for (int p = 0; p < P; p++) {
+                    C fv = fs[p * NB + k];
+                    br[p] += q * fv.x;
+                    bi[p] += q * fv.y;
+                }
+            } else {
+#pragma unroll
+                for (int p = 0; p < P; p++) {
+                    C fv = fs[p * NB + k];
+                    ar[p] += q1 * (q0 * fv.x);
+                    ai[p] += q1 * (q0 * fv.y);
+                }
+            }
+        }
+        if (sizeof(T) == 4) {
+#pragma unroll
+            for (int p = 0; p < P; p++) {
+                kr[p].add(br[p]);
+                ki[p].add(bi[p]);
+            }
+        }
+        __syncwarp();  // stage sb and fs are refilled two steps on
+        if (last) {
+            const int r = v * R + rr;
+#pragma unroll
+            for (int p = 0; p < P; p++) {
+                if (sizeof(T) == 4) {
+                    ar[p] = kr[p].value();
+                    ai[p] = ki[p].value();
+                }
+                S[p * buf + (size_t)cc * n0 + r] = mkc<T>(ar[p], ai[p]);
+                ar[p] = ai[p] = T(0);
+                kr[p].init();
+                ki[p].init();
+            }
+            if (nit < nbands) it_nx = fetch();
+        }
+        it = nit;
+        v = nv;
+        base = nbase;
+        end = nend;
+        sb ^= 1;
+    }
+    cp_async_wait<0>();
     __syncthreads();
     for (int p = 0; p < np; p++) {
         C *G = block_fft<T, +1>(S + p * buf, K, n0, logn0, BC, tw0);
@@ -435,7 +501,7 @@ k_rowifft_crop(const cplx_t<T> *__restrict__ Hp, int N0, int N1, int n1, int log
     for (int idx = threadIdx.x; idx < nr * n1; idx += blockDim.x) A[idx] = Hb[idx];
     __syncthreads();
     C *R = block_fft<T, +1>(A, B, n1, logn1, nr, tw1);
-    double s = 0;
+    T s = 0;
     for (int idx = threadIdx.x; idx < nr * N1; idx += blockDim.x) {
         int r = idx / N1, c = idx - r * N1;
         int a = a0 + r;
@@ -446,11 +512,11 @@ k_rowifft_crop(const cplx_t<T> *__restrict__ Hp, int N0, int N1, int n1, int log
         size_t o = (size_t)gb * ca.out_stride + (size_t)a * N1 + c;
         ca.out[o] = z;
         if (MODE == CM_INIT) ca.p_out[o] = z;
-        s += (double)z.x * z.x + (double)z.y * z.y;
+        s += z.x * z.x + z.y * z.y;
     }
     if (MODE != CM_PLAIN) {
-        s = block_sum(s, sh);
-        if (threadIdx.x == 0) ca.part[(size_t)gb * ca.part_stride + blockIdx.x] = s;
+        double d = block_sum_t<T>(s, sh);
+        if (threadIdx.x == 0) ca.part[(size_t)gb * ca.part_stride + blockIdx.x] = d;
     }
 }
 
@@ -480,7 +546,7 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     if (t.n1 < 4 || t.n0 < 8) return NUDIM_EINVAL;
     const int bca = 4;
     FusedLists L;
-    if (build_fused_lists(t, bc, bca, &L) != 0) {
+    if (build_fused_lists(t, bc, bca, sizeof(T) == 4, &L) != 0) {
         set_error("fused NFFT list construction failed");
         return NUDIM_EINVAL;
     }
@@ -529,6 +595,16 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     NUDIM_TRY(up((void **)&blk_off, L.blk_off.data(), sizeof(int) * L.blk_off.size()));
     NUDIM_TRY(up((void **)&ent, L.ent.data(), sizeof(int) * L.ent.size()));
     NUDIM_TRY(up((void **)&nslots, L.nslots.data(), L.nslots.size()));
+    nE = (int)L.ent.size();
+    NUDIM_TRY(up((void **)&e_rb, L.ent_rb.data(), sizeof(int) * std::max<size_t>(1, L.ent_rb.size())));
+    NUDIM_TRY(up((void **)&e_cc, L.ent_cc.data(), sizeof(int) * std::max<size_t>(1, L.ent_cc.size())));
+    {
+        std::vector<T> qa(L.ent_qa.begin(), L.ent_qa.end()), q1(L.ent_q1.begin(), L.ent_q1.end());
+        if (qa.empty()) qa.assign(16, T(0));
+        if (q1.empty()) q1.assign(1, T(0));
+        NUDIM_TRY(up((void **)&e_qa, qa.data(), sizeof(T) * qa.size()));
+        NUDIM_TRY(up((void **)&e_q1, q1.data(), sizeof(T) * q1.size()));
+    }
     NUDIM_TRY(up((void **)&band_off, L.band_off.data(), sizeof(int) * L.band_off.size()));
     NUDIM_TRY(up((void **)&band_node, L.band_node.data(),
                  sizeof(int) * std::max<size_t>(1, L.band_node.size())));
@@ -568,12 +644,13 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
 
 template <typename T> void NfftDev<T>::release_fused()
 {
-    void *ptrs[] = {tw0, tw1, blk_off, ent, nslots, band_off, band_node, band_ord, band_w};
+    void *ptrs[] = {tw0,      tw1,       blk_off,  ent,    nslots, band_off, band_node,
+                    band_ord, band_w, e_rb, e_cc, e_qa, e_q1};
     for (void *q : ptrs)
         if (q) cudaFreeAsync(q, ast);
     tw0 = tw1 = nullptr;
-    blk_off = ent = band_off = band_node = band_ord = nullptr;
-    band_w = nullptr;
+    blk_off = ent = band_off = band_node = band_ord = e_rb = e_cc = nullptr;
+    band_w = e_qa = e_q1 = nullptr;
     nslots = nullptr;
     fused = false;
 }
@@ -623,7 +700,7 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
             ProfScope ps(ctx, PK_INTERP, st,
                          tab + nb * c * ((double)N0 * n1 + (double)smax * M));
             k_colfft_interp<T><<<dim3(nblk, nb), 32 * col_warps<T>(), smem_col, st>>>(
-                H, N0, n0, logn0, n1, BC, nblk, tw0, u, psi, blk_off, ent, M, smax, P);
+                H, N0, n0, logn0, n1, BC, tw0, blk_off, ent, e_rb, e_cc, e_qa, e_q1, nE, M, smax, P);
             NUDIM_LAUNCH_CHECK();
         }
         {

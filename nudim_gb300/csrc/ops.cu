@@ -13,10 +13,13 @@ k_cg_update(cplx_t<T> *__restrict__ f, const cplx_t<T> *__restrict__ p, cplx_t<T
             const cplx_t<T> *__restrict__ v, const double *__restrict__ dots, int cur, int N,
             int M)
 {
+    // one FP64 division per block (FP64 is slow here), shared with the block
+    __shared__ T s_alpha;
     int b = blockIdx.y;
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double alpha_d = dots[b * 4 + cur] / dots[b * 4 + 2];
-    T alpha = (T)alpha_d;
+    if (threadIdx.x == 0) s_alpha = (T)(dots[b * 4 + cur] / dots[b * 4 + 2]);
+    __syncthreads();
+    const T alpha = s_alpha;
     if (i < (size_t)N) {
         size_t o = (size_t)b * N + i;
         cplx_t<T> fv = f[o], pv = p[o];
@@ -37,10 +40,13 @@ __global__ void __launch_bounds__(256)
 k_cg_pupdate(cplx_t<T> *__restrict__ p, const cplx_t<T> *__restrict__ z,
              const double *__restrict__ dots, int cur, int nxt, int N)
 {
+    __shared__ T s_beta;
     int b = blockIdx.y;
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (threadIdx.x == 0) s_beta = (T)(dots[b * 4 + nxt] / dots[b * 4 + cur]);
+    __syncthreads();
     if (i >= (size_t)N) return;
-    T beta = (T)(dots[b * 4 + nxt] / dots[b * 4 + cur]);
+    const T beta = s_beta;
     size_t o = (size_t)b * N + i;
     cplx_t<T> pv = p[o], zv = z[o];
     p[o] = mkc<T>(beta * pv.x + zv.x, beta * pv.y + zv.y);

@@ -230,7 +230,7 @@ void fft_twiddles(int n, std::vector<double> *tw)
     }
 }
 
-int build_fused_lists(const NfftTables &t, int BC, int BCa, FusedLists *L)
+int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists *L)
 {
     const int kWin = 2 * 6 + 2;
     if (BC <= 0 || t.n1 % BC) return -1;
@@ -268,8 +268,12 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, FusedLists *L)
     // Entry order inside a block (one column-pass lane per entry): entries
     // with equal numbers of window columns inside the block side by side
     // (longest first), so a warp's lanes run equal loops; inside such a run
-    // the first window rows u0 cycle through the 16 residues mod 16, so the
-    // 32 lanes of a warp read shared-memory rows spread over all banks.
+    // the first window rows u0 cycle through the residues mod 16, so the
+    // lanes of a warp read shared-memory rows spread over all banks.  The
+    // column pass reads rows in aligned pairs (pair_rows, 8-byte complex) or
+    // singly (16-byte complex); the residue order puts 8 distinct 16-byte
+    // slots of a 128-byte line in every 8 consecutive lanes.
+    static const int kOrderPairs[16] = {0, 2, 4, 6, 8, 10, 12, 14, 1, 3, 5, 7, 9, 11, 13, 15};
     for (int b = 0; b < nblk; b++) {
         auto cols = [&](int en) {
             int j = en / 8, k = 0;
@@ -289,11 +293,13 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, FusedLists *L)
                 bucket[t.u0[key[q].second / 8] & 15].push_back(key[q].second);
             size_t head[16] = {0};
             for (size_t left = k - i; left > 0;)
-                for (int r = 0; r < 16; r++)
+                for (int q = 0; q < 16; q++) {
+                    int r = pair_rows ? kOrderPairs[q] : q;
                     if (head[r] < bucket[r].size()) {
                         out.push_back(bucket[r][head[r]++]);
                         left--;
                     }
+                }
             i = k;
         }
         per[b] = out;
@@ -303,6 +309,37 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, FusedLists *L)
     L->ent.clear();
     L->ent.reserve(L->blk_off[nblk]);
     for (int b = 0; b < nblk; b++) L->ent.insert(L->ent.end(), per[b].begin(), per[b].end());
+    // per entry, structure of arrays over the nE entries: the even first row
+    // rb of the window, the block columns it covers (first cl0, count cnt;
+    // column q is (cl0 + q) mod BC), 16 row weights aligned to rb (zero
+    // outside the window) and the cnt column weights.
+    const size_t nE = L->ent.size();
+    L->nq = nblk > 1 ? std::min(BC, kWin) : kWin;
+    L->ent_rb.assign(nE, 0);
+    L->ent_cc.assign(nE, 0);
+    L->ent_qa.assign(16 * nE, 0.0);
+    L->ent_q1.assign((size_t)L->nq * nE, 0.0);
+    for (int b = 0; b < nblk; b++)
+        for (int e = L->blk_off[b]; e < L->blk_off[b + 1]; e++) {
+            int j = L->ent[e] / 8, ux = t.u0[j], uy = t.u1[j], col0 = b * BC;
+            int t1lo = 0, cl0 = uy & (n1 - 1), cnt = kWin;
+            if (nblk > 1) {
+                int d = (col0 - uy) & (n1 - 1);
+                cl0 = 0;
+                if (d < kWin) t1lo = d;
+                else cl0 = (uy - col0) & (n1 - 1);
+                cnt = std::min(kWin - t1lo, BC - cl0);
+            }
+            const double *ps = &t.psi[(size_t)j * 2 * kWin];
+            int odd = ux & 1;
+            L->ent_rb[e] = ux - odd;
+            L->ent_cc[e] = cl0 | (cnt << 8);
+            for (int i = 0; i < 16; i++) {
+                int t0 = i - odd;
+                if (t0 >= 0 && t0 < kWin) L->ent_qa[(size_t)i * nE + e] = ps[t0];
+            }
+            for (int q = 0; q < cnt; q++) L->ent_q1[(size_t)q * nE + e] = ps[kWin + t1lo + q];
+        }
     // ---- adjoint lists: tiles of R x BCa grid points (one per warp lane);
     // per tile the nodes whose window meets it, ascending.  Tiles are
     // numbered block-major: tile = b * nbands + v.

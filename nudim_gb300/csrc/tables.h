@@ -47,6 +47,11 @@ struct FusedLists {
     int BCa = 0, nblka = 0, R = 0, nbands = 0;
     std::vector<int> blk_off, ent;          // ent = node * 8 + slot
     std::vector<unsigned char> nslots;      // blocks per node
+    // per trafo entry (structure of arrays over the entries): even first
+    // window row, cl0 | cnt << 8, 16 aligned row weights, nq column weights
+    int nq = 0;
+    std::vector<int> ent_rb, ent_cc;
+    std::vector<double> ent_qa, ent_q1;
     std::vector<int> band_off, band_node;   // CSR over tiles b * nbands + v
     std::vector<double> band_w;             // per entry R row + BCa column weights
     std::vector<int> band_ord;              // per block its tiles, longest list first
@@ -55,7 +60,7 @@ struct FusedLists {
 // BC a power of two dividing n1; BCa a power of two <= 32 dividing n1.
 // Returns 0, -1 (bad shape) or -2 (a window meets one trafo block twice:
 // the grid is too narrow for column blocks of BC).
-int build_fused_lists(const NfftTables &t, int BC, int BCa, FusedLists *L);
+int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists *L);
 
 // e^{-2 pi i k / n}, k < n, interleaved (re, im)
 void fft_twiddles(int n, std::vector<double> *tw);
