@@ -458,15 +458,29 @@ static int validate(const nudim_job_desc *d)
     return NUDIM_OK;
 }
 
-static size_t job_bytes(const nudim_job_desc *d, int A, bool both)
+// scratch of one fused NFFT pass (row spectra + partials of a chunk of planes):
+// NUDIM_FUSED_BUDGET_MB, default 1.5 GB (all Z-planes of most jobs in one pass)
+static size_t fused_budget_default()
+{
+    const char *fb = getenv("NUDIM_FUSED_BUDGET_MB");
+    return fb ? (size_t)atol(fb) << 20 : ((size_t)1536 << 20);
+}
+
+static size_t job_bytes(const nudim_job_desc *d, int A, bool both, size_t fused_budget)
 {
     size_t nz = d->nz, np = d->np, P2 = np * np, V = P2 * nz, M = (size_t)A * np;
+    size_t n1 = (size_t)grid_size(d->np);
     auto per = [&](size_t sT) {
         size_t sC = 2 * sT;
         size_t b = 2 * V * sT + 3 * V * sC + 4 * nz * M * sC;
         if (d->denoise == NUDIM_DENOISE_TV) b += V * sT;
         b += M * (8 + 28 * sT + 20);  // node tables and tile lists
+        // fused-path lists: ~11 adjoint tile entries and <= 3 trafo entries per node
+        b += M * (11 * (4 + 12 * sT) + 3 * (8 + 24 * sT));
         b += nz * (size_t)cgnr_part_stride((int)M, (int)P2) * 8;
+        // fused-path workspace: row spectra + partials of one chunk of planes
+        size_t plane = (np * n1 + 3 * M) * sC, chunk = fused_budget / plane;
+        b += (chunk < 1 ? 1 : chunk < nz ? chunk : nz) * plane;
         return b;
     };
     size_t b = d->precision == NUDIM_FP64 ? per(8) : per(4);
@@ -505,8 +519,7 @@ int nudim_ctx_create(int device, unsigned flags, nudim_ctx **out)
     }
     const char *gb = getenv("NUDIM_GRID_BUDGET_MB");
     c->grid_budget = gb ? (size_t)atol(gb) << 20 : ((size_t)2 << 30);
-    const char *fb = getenv("NUDIM_FUSED_BUDGET_MB");
-    c->fused_budget = fb ? (size_t)atol(fb) << 20 : ((size_t)96 << 20);
+    c->fused_budget = fused_budget_default();
     c->use_fused = !(flags & NUDIM_CTX_GRID_NFFT);
     *out = c;
     return NUDIM_OK;
@@ -588,7 +601,8 @@ int nudim_job_footprint(const nudim_job_desc *d, size_t *bytes)
 {
     NUDIM_TRY(validate(d));
     int A = polar_lines(d->gam_min, d->interval, d->padangle, nullptr, nullptr);
-    *bytes = job_bytes(d, A, d->precision == NUDIM_MIXED && d->correct_every > 0);
+    *bytes = job_bytes(d, A, d->precision == NUDIM_MIXED && d->correct_every > 0,
+                       fused_budget_default());
     return NUDIM_OK;
 }
 

@@ -31,71 +31,167 @@ __device__ __forceinline__ cplx_t<T> cmul(cplx_t<T> a, cplx_t<T> b)
     return mkc<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// `cnt` FFTs of length n = 2^logn stored back to back in a; b is scratch of
-// the same size.  DIR = -1 forward (e^{-2 pi i}), +1 inverse; unnormalised.
-// Stockham autosort (radix 4, one radix-2 stage when logn is odd).  tw holds
-// e^{-2 pi i t/n}.  All threads of the block call it; returns the buffer that
-// holds the result.
+// `cnt` FFTs of length n = 2^logn stored back to back in a; b is scratch.
+// DIR = -1 forward (e^{-2 pi i}), +1 inverse; unnormalised.  Stockham
+// autosort with radix-16 passes (a radix-8/4/2 pass last when 4 does not
+// divide logn): each thread loads R elements at stride n/R, applies the
+// twiddles e^{-2 pi i m k / (R Ns)} (table tw: e^{-2 pi i t/n}), does an
+// R-point DFT in registers and stores R outputs at stride Ns.  Between
+// passes the buffers hold element i at i + i/16, so the strided stores of
+// the first passes meet distinct banks; the first pass reads and the last
+// pass writes the plain layout.  Both buffers need fft_buf(cnt * n)
+// elements.  All threads of the block call it; returns the buffer that
+// holds the result (plain layout).
+__host__ __device__ constexpr size_t fft_buf(size_t elems) { return elems + (elems >> 4); }
+__device__ __forceinline__ int fft_pad(int i) { return i + (i >> 4); }
+
+// e^{DIR 2 pi i k / 16}, k < 16, from cos(2 pi k / 16) for k = 0..4
+template <typename T, int DIR> __device__ __forceinline__ cplx_t<T> w16(int k)
+{
+    constexpr double c[5] = {1.0, 0.92387953251128675613, 0.70710678118654752440,
+                             0.38268343236508977173, 0.0};
+    double cs, sn;
+    int q = k & 3, h = k >> 2;  // k = 4h + q: rotate (cos, sin) of q by h quarter turns
+    double cq = c[q], sq = c[4 - q];
+    switch (h & 3) {
+    case 0: cs = cq; sn = sq; break;
+    case 1: cs = -sq; sn = cq; break;
+    case 2: cs = -cq; sn = -sq; break;
+    default: cs = sq; sn = -cq; break;
+    }
+    return mkc<T>((T)cs, (T)(DIR * sn));
+}
+
+template <typename T, int DIR>
+__device__ __forceinline__ void dft2(cplx_t<T> &a0, cplx_t<T> &a1)
+{
+    cplx_t<T> t = a0;
+    a0 = mkc<T>(t.x + a1.x, t.y + a1.y);
+    a1 = mkc<T>(t.x - a1.x, t.y - a1.y);
+}
+
+template <typename T, int DIR>
+__device__ __forceinline__ void dft4(cplx_t<T> &x0, cplx_t<T> &x1, cplx_t<T> &x2, cplx_t<T> &x3)
+{
+    using C = cplx_t<T>;
+    C a0 = mkc<T>(x0.x + x2.x, x0.y + x2.y), a1 = mkc<T>(x0.x - x2.x, x0.y - x2.y);
+    C a2 = mkc<T>(x1.x + x3.x, x1.y + x3.y), a3 = mkc<T>(x1.x - x3.x, x1.y - x3.y);
+    x0 = mkc<T>(a0.x + a2.x, a0.y + a2.y);
+    x2 = mkc<T>(a0.x - a2.x, a0.y - a2.y);
+    // forward: X1 = a1 - i a3, X3 = a1 + i a3; inverse: the other way
+    if (DIR < 0) {
+        x1 = mkc<T>(a1.x + a3.y, a1.y - a3.x);
+        x3 = mkc<T>(a1.x - a3.y, a1.y + a3.x);
+    } else {
+        x1 = mkc<T>(a1.x - a3.y, a1.y + a3.x);
+        x3 = mkc<T>(a1.x + a3.y, a1.y - a3.x);
+    }
+}
+
+// R-point DFT of a[0..R) in registers.  Output X[p] is left in a[out(p)]:
+// R = 16 and 8 are split as R1 = 4 inner DFTs over m = R2 m1 + m2, the
+// twiddles e^{DIR 2 pi i m2 p1 / R} and R2-point outer DFTs, X[p1 + 4 p2] in
+// a[R2 p1 + p2].
+template <int R> __device__ __forceinline__ constexpr int dft_out(int p)
+{
+    return R == 16 ? 4 * (p & 3) + (p >> 2) : R == 8 ? 2 * (p & 3) + (p >> 2) : p;
+}
+
+template <typename T, int DIR, int R> __device__ __forceinline__ void dft_regs(cplx_t<T> *a)
+{
+    if (R == 2) {
+        dft2<T, DIR>(a[0], a[1]);
+    } else if (R == 4) {
+        dft4<T, DIR>(a[0], a[1], a[2], a[3]);
+    } else if (R == 8) {
+#pragma unroll
+        for (int m2 = 0; m2 < 2; m2++) dft4<T, DIR>(a[m2], a[2 + m2], a[4 + m2], a[6 + m2]);
+#pragma unroll
+        for (int p1 = 1; p1 < 4; p1++) a[2 * p1 + 1] = cmul<T>(a[2 * p1 + 1], w16<T, DIR>(2 * p1));
+#pragma unroll
+        for (int p1 = 0; p1 < 4; p1++) dft2<T, DIR>(a[2 * p1], a[2 * p1 + 1]);
+    } else {
+#pragma unroll
+        for (int m2 = 0; m2 < 4; m2++)
+            dft4<T, DIR>(a[m2], a[4 + m2], a[8 + m2], a[12 + m2]);
+#pragma unroll
+        for (int p1 = 1; p1 < 4; p1++)
+#pragma unroll
+            for (int m2 = 1; m2 < 4; m2++)
+                a[4 * p1 + m2] = cmul<T>(a[4 * p1 + m2], w16<T, DIR>(m2 * p1));
+#pragma unroll
+        for (int p1 = 0; p1 < 4; p1++)
+            dft4<T, DIR>(a[4 * p1], a[4 * p1 + 1], a[4 * p1 + 2], a[4 * p1 + 3]);
+    }
+}
+
+template <typename T, int DIR, int R, bool IN_PAD, bool OUT_PAD>
+__device__ __forceinline__ void fft_pass(const cplx_t<T> *__restrict__ x, cplx_t<T> *__restrict__ y,
+                                         int n, int lognR, int Ns, int cnt,
+                                         const cplx_t<T> *__restrict__ tw)
+{
+    using C = cplx_t<T>;
+    const int nR = 1 << lognR, step = n / (R * Ns);
+    for (int q = threadIdx.x; q < cnt * nR; q += blockDim.x) {
+        const int s = q >> lognR, j = q & (nR - 1), k = j & (Ns - 1);
+        const int base = s * n;
+        C a[R];
+#pragma unroll
+        for (int m = 0; m < R; m++) {
+            int i = base + j + m * nR;
+            a[m] = x[IN_PAD ? fft_pad(i) : i];
+        }
+        if (Ns > 1) {
+            const int ks = k * step;
+#pragma unroll
+            for (int m = 1; m < R; m++) {
+                C w = tw[m * ks];
+                if (DIR > 0) w.y = -w.y;
+                a[m] = cmul<T>(a[m], w);
+            }
+        }
+        dft_regs<T, DIR, R>(a);
+        const int ob = base + (j - k) * R + k;
+#pragma unroll
+        for (int p = 0; p < R; p++) {
+            int i = ob + p * Ns;
+            y[OUT_PAD ? fft_pad(i) : i] = a[dft_out<R>(p)];
+        }
+    }
+}
+
+template <typename T, int DIR, int R>
+__device__ __forceinline__ void fft_pass_sel(const cplx_t<T> *x, cplx_t<T> *y, int n, int lognR,
+                                             int Ns, int cnt, const cplx_t<T> *tw, bool first,
+                                             bool last)
+{
+    if (first && last) fft_pass<T, DIR, R, false, false>(x, y, n, lognR, Ns, cnt, tw);
+    else if (first) fft_pass<T, DIR, R, false, true>(x, y, n, lognR, Ns, cnt, tw);
+    else if (last) fft_pass<T, DIR, R, true, false>(x, y, n, lognR, Ns, cnt, tw);
+    else fft_pass<T, DIR, R, true, true>(x, y, n, lognR, Ns, cnt, tw);
+}
+
 template <typename T, int DIR>
 __device__ cplx_t<T> *block_fft(cplx_t<T> *a, cplx_t<T> *b, int n, int logn, int cnt,
                                 const cplx_t<T> *__restrict__ tw)
 {
-    using C = cplx_t<T>;
-    const int nthr = blockDim.x, tid = threadIdx.x;
-    int Ns = 1;
-    if (logn & 1) {
-        const int half = n >> 1;
-        for (int q = tid; q < cnt * half; q += nthr) {
-            int s = q >> (logn - 1), j = q & (half - 1);
-            const C *x = a + (size_t)s * n;
-            C *y = b + (size_t)s * n;
-            C v0 = x[j], v1 = x[j + half];
-            y[2 * j] = mkc<T>(v0.x + v1.x, v0.y + v1.y);
-            y[2 * j + 1] = mkc<T>(v0.x - v1.x, v0.y - v1.y);
+    const int npass = (logn + 3) >> 2;
+    int rem = logn, Ns = 1;
+    for (int t = 0; t < npass; t++) {
+        const int lr = rem < 4 ? rem : 4;
+        const bool first = t == 0, last = t == npass - 1;
+        const int lognR = logn - lr;
+        switch (lr) {
+        case 4: fft_pass_sel<T, DIR, 16>(a, b, n, lognR, Ns, cnt, tw, first, last); break;
+        case 3: fft_pass_sel<T, DIR, 8>(a, b, n, lognR, Ns, cnt, tw, first, last); break;
+        case 2: fft_pass_sel<T, DIR, 4>(a, b, n, lognR, Ns, cnt, tw, first, last); break;
+        default: fft_pass_sel<T, DIR, 2>(a, b, n, lognR, Ns, cnt, tw, first, last); break;
         }
-        C *t = a;
+        rem -= lr;
+        Ns <<= lr;
+        cplx_t<T> *t2 = a;
         a = b;
-        b = t;
-        Ns = 2;
-        __syncthreads();
-    }
-    const int quarter = n >> 2;
-    for (; Ns < n; Ns <<= 2) {
-        const int step = n / (4 * Ns);
-        for (int q = tid; q < cnt * quarter; q += nthr) {
-            int s = q >> (logn - 2), j = q & (quarter - 1);
-            const C *x = a + (size_t)s * n;
-            C *y = b + (size_t)s * n;
-            int k = j & (Ns - 1);
-            C v0 = x[j], v1 = x[j + quarter], v2 = x[j + 2 * quarter], v3 = x[j + 3 * quarter];
-            if (Ns > 1) {
-                C w1 = tw[k * step], w2 = tw[2 * k * step], w3 = tw[3 * k * step];
-                if (DIR > 0) {
-                    w1.y = -w1.y;
-                    w2.y = -w2.y;
-                    w3.y = -w3.y;
-                }
-                v1 = cmul<T>(v1, w1);
-                v2 = cmul<T>(v2, w2);
-                v3 = cmul<T>(v3, w3);
-            }
-            C a0 = mkc<T>(v0.x + v2.x, v0.y + v2.y), a1 = mkc<T>(v0.x - v2.x, v0.y - v2.y);
-            C a2 = mkc<T>(v1.x + v3.x, v1.y + v3.y), a3 = mkc<T>(v1.x - v3.x, v1.y - v3.y);
-            int o = (j - k) * 4 + k;
-            y[o] = mkc<T>(a0.x + a2.x, a0.y + a2.y);
-            y[o + 2 * Ns] = mkc<T>(a0.x - a2.x, a0.y - a2.y);
-            // forward: X1 = a1 - i a3, X3 = a1 + i a3; inverse: the other way
-            if (DIR < 0) {
-                y[o + Ns] = mkc<T>(a1.x + a3.y, a1.y - a3.x);
-                y[o + 3 * Ns] = mkc<T>(a1.x - a3.y, a1.y + a3.x);
-            } else {
-                y[o + Ns] = mkc<T>(a1.x - a3.y, a1.y + a3.x);
-                y[o + 3 * Ns] = mkc<T>(a1.x + a3.y, a1.y - a3.x);
-            }
-        }
-        C *t = a;
-        a = b;
-        b = t;
+        b = t2;
         __syncthreads();
     }
     return a;
@@ -112,7 +208,7 @@ k_rowfft(const void *__restrict__ src, size_t src_stride, int N0, int N1, int n1
 {
     using C = cplx_t<T>;
     extern __shared__ __align__(16) unsigned char smraw[];
-    C *A = (C *)smraw, *B = A + kRows * n1;
+    C *A = (C *)smraw, *B = A + fft_buf((size_t)kRows * n1);
     int b = blockIdx.y, gb = plane0 + b, a0 = blockIdx.x * kRows;
     int nr = min(kRows, N0 - a0);
     for (int idx = threadIdx.x; idx < nr * n1; idx += blockDim.x) {
@@ -141,8 +237,9 @@ k_rowfft(const void *__restrict__ src, size_t src_stride, int N0, int N1, int n1
 }
 
 // ================================================================ K2 column pass + interpolation
-// warps per trafo column-block CTA (FP64: fewer, with room for the row weights)
-template <typename T> __host__ __device__ constexpr int col_warps() { return sizeof(T) == 4 ? 32 : 16; }
+// warps per trafo column-block CTA (register room for the radix-16 FFT passes
+// and the row weights)
+template <typename T> __host__ __device__ constexpr int col_warps() { return sizeof(T) == 4 ? 16 : 8; }
 
 // Shared memory: two BC x n0 complex buffers (FFT).  After the column FFTs
 // each lane takes one (node, block) entry of the block's list and sums the
@@ -164,7 +261,7 @@ k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int 
 {
     using C = cplx_t<T>;
     extern __shared__ __align__(16) unsigned char smraw[];
-    C *A = (C *)smraw, *B = A + (size_t)BC * n0;
+    C *A = (C *)smraw, *B = A + fft_buf((size_t)BC * n0);
     int cb = blockIdx.x, b = blockIdx.y;
     const C *Hb = H + (size_t)b * N0 * n1 + (size_t)cb * BC;
     // rows a of H land at l0 = (a - N0/2) mod n0; the other rows are zero
@@ -328,7 +425,7 @@ k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
     constexpr int TV = 16 / sizeof(T);  // weights per 16-byte copy
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ int next_tile, s_off[kMaxBands + 1], s_ord[kMaxBands];
-    const size_t buf = (size_t)BC * n0;
+    const size_t buf = fft_buf((size_t)BC * n0);  // S_p and K, each with the FFT's padding
     C *S = (C *)smraw, *K = S + P * buf;
     const int cb = blockIdx.x, pb = blockIdx.y * P;
     const int np = min(P, nb_planes - pb);
@@ -494,7 +591,7 @@ k_rowifft_crop(const cplx_t<T> *__restrict__ Hp, int N0, int N1, int n1, int log
     using C = cplx_t<T>;
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double sh[32];
-    C *A = (C *)smraw, *B = A + kRows * n1;
+    C *A = (C *)smraw, *B = A + fft_buf((size_t)kRows * n1);
     int b = blockIdx.y, gb = plane0 + b, a0 = blockIdx.x * kRows;
     int nr = min(kRows, N0 - a0);
     const C *Hb = Hp + ((size_t)b * N0 + a0) * n1;
@@ -557,15 +654,15 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     nblka = L.nblka;
     nbands = L.nbands;
     if (nbands > kMaxBands) return NUDIM_EINVAL;
-    // rows per CTA in the row passes: two rows x n1 complex buffers within 112 KB
-    rows = (int)((112 << 10) / (2 * sizeof(C) * (size_t)t.n1));
-    if (rows > 4) rows = 4;
-    smem_col = 2 * sizeof(C) * (size_t)BC * n0;
-    smem_row = 2 * sizeof(C) * (size_t)rows * n1;
+    // rows per CTA in the row passes: two (padded) rows x n1 complex buffers within 112 KB
+    rows = 4;
+    while (rows > 1 && 2 * sizeof(C) * fft_buf((size_t)rows * t.n1) > ((size_t)112 << 10)) rows--;
+    smem_col = 2 * sizeof(C) * fft_buf((size_t)BC * n0);
+    smem_row = 2 * sizeof(C) * fft_buf((size_t)rows * n1);
     // adjoint column pass: as many planes per CTA (4, 2, 1) as fit in 212 KB
     // of dynamic shared memory (8 KB of tile offsets and order are static)
     const int Wa = 32 / BCa + BCa;
-    size_t bufa = sizeof(C) * (size_t)BCa * n0;
+    size_t bufa = sizeof(C) * fft_buf((size_t)BCa * n0);
     auto spread_smem = [&](int p) -> size_t {
         size_t st = p == 4 ? spread_stage_bytes<T, 4>(Wa)
                   : p == 2 ? spread_stage_bytes<T, 2>(Wa) : spread_stage_bytes<T, 1>(Wa);
@@ -576,7 +673,7 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     smem_spread = spread_smem(Pa);
     // The limit is a property of the kernel, shared by every plan in the
     // process: set it to the largest size any plan uses (never lower it).
-    const int lim_col = 128 << 10, lim_row = 112 << 10, lim_spread = 212 << 10;
+    const int lim_col = 144 << 10, lim_row = 112 << 10, lim_spread = 212 << 10;
     if (rows < 1 || smem_col > (size_t)lim_col || smem_row > (size_t)lim_row ||
         smem_spread > (size_t)lim_spread) {
         set_error("fused NFFT: shared memory plan exceeds the kernel limits");
@@ -658,7 +755,7 @@ template <typename T> void NfftDev<T>::release_fused()
 template <typename T> int NfftDev<T>::fused_chunk(int nplanes) const
 {
     size_t per = sizeof(C) * ((size_t)N0 * n1 + (size_t)smax * M);
-    size_t budget = ctx->fused_budget ? ctx->fused_budget : ((size_t)96 << 20);
+    size_t budget = ctx->fused_budget ? ctx->fused_budget : ((size_t)1536 << 20);
     long c = (long)(budget / per);
     if (c < 1) c = 1;
     if (c > nplanes) c = nplanes;
