@@ -223,23 +223,32 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
             int g_hi = min(gc - 1, t / 2);
             int a = t - (D - 1);
             int g_lo = a > 0 ? (a + 1) / 2 : 0;
-            // P threads per diagonal, gs diagonals at a time
-            for (int g = g_lo + gi; gi < gs && g <= g_hi; g += gs) {
-                const int d = t - 2 * g;
-                const int yd = y0(d), nd = len(d);
-                const int ym = y0(d > 0 ? d - 1 : d), yp = y0(d + 1);
-                T *sc = slot(d);
-                const T *sm = slot(d > 0 ? d - 1 : d), *sp = slot(d + 1);
-                for (int i = i0; i < nd; i += P) {
-                    int y = yd + i, x = d - y;
-                    T cv = sc[i];
-                    T nN = cv, nS = cv, nW = cv, nE = cv;
-                    if (y > 0) nN = sm[(y - 1) - ym];
-                    if (x > 0) nW = sm[y - ym];
-                    if (y < ny - 1) nS = sp[(y + 1) - yp];
-                    int ip = (x == nxb - 1) ? nxb - 1 : x + 1;
-                    if (ip != x) nE = ip < nx ? sp[y - yp] : T(0);
-                    sc[i] = diff_cell<T>(cv, nN, nS, nE, nW, lambda, Ksq);
+            // P threads per diagonal, gs diagonals at a time; the ring slot of
+            // diagonal d = t - 2g moves down by 2 gs per g (no division)
+            if (gi < gs && g_lo + gi <= g_hi) {
+                int sd = (t - 2 * (g_lo + gi)) % R;
+                for (int g = g_lo + gi; g <= g_hi; g += gs) {
+                    const int d = t - 2 * g;
+                    const int yd = y0(d), nd = min(d, ny - 1) - yd + 1;
+                    if (i0 < nd) {
+                        T *sc = ring + (size_t)sd * L;
+                        const T *sm = d > 0 ? ring + (size_t)(sd == 0 ? R - 1 : sd - 1) * L : sc;
+                        const T *sp = ring + (size_t)(sd == R - 1 ? 0 : sd + 1) * L;
+                        const int ym = y0(d > 0 ? d - 1 : d), yp = y0(d + 1);
+                        for (int i = i0; i < nd; i += P) {
+                            int y = yd + i, x = d - y;
+                            T cv = sc[i];
+                            T nN = cv, nS = cv, nW = cv, nE = cv;
+                            if (y > 0) nN = sm[(y - 1) - ym];
+                            if (x > 0) nW = sm[y - ym];
+                            if (y < ny - 1) nS = sp[(y + 1) - yp];
+                            int ip = (x == nxb - 1) ? nxb - 1 : x + 1;
+                            if (ip != x) nE = ip < nx ? sp[y - yp] : T(0);
+                            sc[i] = diff_cell<T>(cv, nN, nS, nE, nW, lambda, Ksq);
+                        }
+                    }
+                    sd -= 2 * gs;
+                    if (sd < 0) sd += R;
                 }
             }
             if (nn > 0) {
