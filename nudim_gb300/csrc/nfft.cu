@@ -211,11 +211,12 @@ int NfftDev<T>::init(nudim_ctx *c, const NfftTables &t, cudaStream_t st, Workspa
     if (c->use_fused && init_fused(t, st) == NUDIM_OK) return NUDIM_OK;
     fused = false;
     // grid path: tile lists of the spreading gather
-    NUDIM_TRY(upload_async((void **)&tile_off, t.tile_off.data(),
-                           sizeof(int) * t.tile_off.size(), st));
-    NUDIM_TRY(upload_async((void **)&tile_nodes, t.tile_nodes.data(),
-                           sizeof(int) * t.tile_nodes.size(), st));
-    bytes += sizeof(int) * (t.tile_off.size() + t.tile_nodes.size());
+    std::vector<int> toff, tnodes;
+    build_tile_lists(t, &toff, &tnodes);
+    if (tnodes.empty()) tnodes.assign(1, 0);
+    NUDIM_TRY(upload_async((void **)&tile_off, toff.data(), sizeof(int) * toff.size(), st));
+    NUDIM_TRY(upload_async((void **)&tile_nodes, tnodes.data(), sizeof(int) * tnodes.size(), st));
+    bytes += sizeof(int) * (toff.size() + tnodes.size());
     return NUDIM_OK;
 }
 

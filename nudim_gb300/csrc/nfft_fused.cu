@@ -642,7 +642,7 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     // 12 weights move as 16-byte vectors)
     if (t.n1 < 4 || t.n0 < 8) return NUDIM_EINVAL;
     const int bca = 4;
-    FusedLists L;
+    FusedLists<T> L;
     if (build_fused_lists(t, bc, bca, sizeof(T) == 4, &L) != 0) {
         set_error("fused NFFT list construction failed");
         return NUDIM_EINVAL;
@@ -693,24 +693,17 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     NUDIM_TRY(up((void **)&ent, L.ent.data(), sizeof(int) * L.ent.size()));
     NUDIM_TRY(up((void **)&nslots, L.nslots.data(), L.nslots.size()));
     nE = (int)L.ent.size();
-    NUDIM_TRY(up((void **)&e_rb, L.ent_rb.data(), sizeof(int) * std::max<size_t>(1, L.ent_rb.size())));
-    NUDIM_TRY(up((void **)&e_cc, L.ent_cc.data(), sizeof(int) * std::max<size_t>(1, L.ent_cc.size())));
-    {
-        std::vector<T> qa(L.ent_qa.begin(), L.ent_qa.end()), q1(L.ent_q1.begin(), L.ent_q1.end());
-        if (qa.empty()) qa.assign(16, T(0));
-        if (q1.empty()) q1.assign(1, T(0));
-        NUDIM_TRY(up((void **)&e_qa, qa.data(), sizeof(T) * qa.size()));
-        NUDIM_TRY(up((void **)&e_q1, q1.data(), sizeof(T) * q1.size()));
-    }
+    if (L.ent_rb.empty()) L.ent_rb.assign(1, 0);
+    if (L.ent_cc.empty()) L.ent_cc.assign(1, 0);
+    NUDIM_TRY(up((void **)&e_rb, L.ent_rb.data(), sizeof(int) * L.ent_rb.size()));
+    NUDIM_TRY(up((void **)&e_cc, L.ent_cc.data(), sizeof(int) * L.ent_cc.size()));
+    NUDIM_TRY(up((void **)&e_qa, L.ent_qa.data(), sizeof(T) * L.ent_qa.size()));
+    NUDIM_TRY(up((void **)&e_q1, L.ent_q1.data(), sizeof(T) * L.ent_q1.size()));
     NUDIM_TRY(up((void **)&band_off, L.band_off.data(), sizeof(int) * L.band_off.size()));
     NUDIM_TRY(up((void **)&band_node, L.band_node.data(),
                  sizeof(int) * std::max<size_t>(1, L.band_node.size())));
     NUDIM_TRY(up((void **)&band_ord, L.band_ord.data(), sizeof(int) * L.band_ord.size()));
-    {
-        std::vector<T> bw(L.band_w.begin(), L.band_w.end());
-        if (bw.empty()) bw.assign(Wa, T(0));
-        NUDIM_TRY(up((void **)&band_w, bw.data(), sizeof(T) * bw.size()));
-    }
+    NUDIM_TRY(up((void **)&band_w, L.band_w.data(), sizeof(T) * L.band_w.size()));
     NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     lim_col));
     NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, true, 1>,

@@ -5,11 +5,30 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <thread>
 
 namespace nudim {
 
 static constexpr int kM = 6;
 static constexpr int kW = 2 * kM + 2;
+
+// fn(begin, end, part) over [0, n) split into contiguous parts, one host
+// thread each (at most 16; one part for small n).  Parts are ordered:
+// part k covers indices below those of part k + 1.
+template <typename F> static int parallel_for(int n, int grain, F &&fn)
+{
+    int hw = (int)std::thread::hardware_concurrency();
+    int nt = std::max(1, std::min({16, hw > 0 ? hw : 1, n / std::max(1, grain)}));
+    if (nt == 1) {
+        fn(0, n, 0);
+        return 1;
+    }
+    std::vector<std::thread> th;
+    for (int k = 0; k < nt; k++)
+        th.emplace_back([&, k] { fn((int)((long)n * k / nt), (int)((long)n * (k + 1) / nt), k); });
+    for (auto &x : th) x.join();
+    return nt;
+}
 
 int grid_size(int N)
 {
@@ -118,34 +137,41 @@ int build_nfft_tables(int N0, int N1, int M, const double *x, int ty, int tx, Nf
     t->u0.assign(M, 0);
     t->u1.assign(M, 0);
     t->psi.assign((size_t)M * 2 * kW, 0.0);
-    for (int j = 0; j < M; j++) {
-        for (int d = 0; d < 2; d++) {
-            int n = d ? t->n1 : t->n0;
-            double b = d ? b1 : b0;
-            double xn = x[2 * (size_t)j + d] * (double)n;
-            int u = (int)floor(xn) - kM;
-            (d ? t->u1 : t->u0)[j] = u;
-            double *ps = t->psi.data() + (size_t)j * 2 * kW + (size_t)d * kW;
-            for (int s = 0; s < kW; s++) ps[s] = kb_phi(xn - (double)(u + s), b);
+    parallel_for(M, 2048, [&](int j0, int j1, int) {
+        for (int j = j0; j < j1; j++) {
+            for (int d = 0; d < 2; d++) {
+                int n = d ? t->n1 : t->n0;
+                double b = d ? b1 : b0;
+                double xn = x[2 * (size_t)j + d] * (double)n;
+                int u = (int)floor(xn) - kM;
+                (d ? t->u1 : t->u0)[j] = u;
+                double *ps = t->psi.data() + (size_t)j * 2 * kW + (size_t)d * kW;
+                for (int s = 0; s < kW; s++) ps[s] = kb_phi(xn - (double)(u + s), b);
+            }
         }
-    }
+    });
     t->c0.resize(N0);
     t->c1.resize(N1);
     for (int k = 0; k < N0; k++) t->c0[k] = 1.0 / kb_phi_hat(k - N0 / 2, t->n0, b0);
     for (int k = 0; k < N1; k++) t->c1[k] = 1.0 / kb_phi_hat(k - N1 / 2, t->n1, b1);
 
-    // tile lists for the atomic-free gather form of the adjoint
     t->ty = std::min(ty, t->n0);
     t->tx = std::min(tx, t->n1);
     t->nty = t->n0 / t->ty;
     t->ntx = t->n1 / t->tx;
-    int ntiles = t->nty * t->ntx;
+    return 0;
+}
+
+void build_tile_lists(const NfftTables &t, std::vector<int> *off, std::vector<int> *nodes)
+{
+    const int M = t.M;
+    int ntiles = t.nty * t.ntx;
     std::vector<int> cnt(ntiles + 1, 0);
     auto visit = [&](int j, auto &&fn) {
         int rows[16], cols[16], nr = 0, nc = 0;
         for (int s = 0; s < kW; s++) {
-            int r = ((t->u0[j] + s) & (t->n0 - 1)) / t->ty;
-            int c = ((t->u1[j] + s) & (t->n1 - 1)) / t->tx;
+            int r = ((t.u0[j] + s) & (t.n0 - 1)) / t.ty;
+            int c = ((t.u1[j] + s) & (t.n1 - 1)) / t.tx;
             bool hr = false, hc = false;
             for (int q = 0; q < nr; q++) hr |= rows[q] == r;
             for (int q = 0; q < nc; q++) hc |= cols[q] == c;
@@ -153,15 +179,14 @@ int build_nfft_tables(int N0, int N1, int M, const double *x, int ty, int tx, Nf
             if (!hc && nc < 16) cols[nc++] = c;
         }
         for (int a = 0; a < nr; a++)
-            for (int c = 0; c < nc; c++) fn(rows[a] * t->ntx + cols[c]);
+            for (int c = 0; c < nc; c++) fn(rows[a] * t.ntx + cols[c]);
     };
     for (int j = 0; j < M; j++) visit(j, [&](int tile) { cnt[tile + 1]++; });
     for (int i = 0; i < ntiles; i++) cnt[i + 1] += cnt[i];
-    t->tile_off = cnt;
-    t->tile_nodes.assign(cnt[ntiles], 0);
+    *off = cnt;
+    nodes->assign(cnt[ntiles], 0);
     std::vector<int> pos(cnt.begin(), cnt.end() - 1);
-    for (int j = 0; j < M; j++) visit(j, [&](int tile) { t->tile_nodes[pos[tile]++] = j; });
-    return 0;
+    for (int j = 0; j < M; j++) visit(j, [&](int tile) { (*nodes)[pos[tile]++] = j; });
 }
 
 void cgnr_weights(int A, int np, double padangle, double *w)
@@ -230,7 +255,8 @@ void fft_twiddles(int n, std::vector<double> *tw)
     }
 }
 
-int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists *L)
+template <typename Wt>
+int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists<Wt> *L)
 {
     const int kWin = 2 * 6 + 2;
     if (BC <= 0 || t.n1 % BC) return -1;
@@ -274,7 +300,8 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
     // singly (16-byte complex); the residue order puts 8 distinct 16-byte
     // slots of a 128-byte line in every 8 consecutive lanes.
     static const int kOrderPairs[16] = {0, 2, 4, 6, 8, 10, 12, 14, 1, 3, 5, 7, 9, 11, 13, 15};
-    for (int b = 0; b < nblk; b++) {
+    parallel_for(nblk, 1, [&](int b0, int b1, int) {
+    for (int b = b0; b < b1; b++) {
         auto cols = [&](int en) {
             int j = en / 8, k = 0;
             for (int s = 0; s < kWin; s++) k += ((t.u1[j] + s) & (n1 - 1)) / BC == b;
@@ -304,6 +331,7 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
         }
         per[b] = out;
     }
+    });
     L->blk_off.assign(nblk + 1, 0);
     for (int b = 0; b < nblk; b++) L->blk_off[b + 1] = L->blk_off[b] + (int)per[b].size();
     L->ent.clear();
@@ -317,9 +345,12 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
     L->nq = nblk > 1 ? std::min(BC, kWin) : kWin;
     L->ent_rb.assign(nE, 0);
     L->ent_cc.assign(nE, 0);
-    L->ent_qa.assign(16 * nE, 0.0);
-    L->ent_q1.assign((size_t)L->nq * nE, 0.0);
-    for (int b = 0; b < nblk; b++)
+    L->ent_qa.alloc(16 * nE);
+    L->ent_q1.alloc((size_t)L->nq * nE);
+    Wt *qa = L->ent_qa.data(), *q1 = L->ent_q1.data();
+    const int nq = L->nq;
+    parallel_for(nblk, 1, [&](int b0, int b1, int) {
+    for (int b = b0; b < b1; b++)
         for (int e = L->blk_off[b]; e < L->blk_off[b + 1]; e++) {
             int j = L->ent[e] / 8, ux = t.u0[j], uy = t.u1[j], col0 = b * BC;
             int t1lo = 0, cl0 = uy & (n1 - 1), cnt = kWin;
@@ -336,18 +367,19 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
             L->ent_cc[e] = cl0 | (cnt << 8);
             for (int i = 0; i < 16; i++) {
                 int t0 = i - odd;
-                if (t0 >= 0 && t0 < kWin) L->ent_qa[(size_t)i * nE + e] = ps[t0];
+                qa[(size_t)i * nE + e] = (Wt)(t0 >= 0 && t0 < kWin ? ps[t0] : 0.0);
             }
-            for (int q = 0; q < cnt; q++) L->ent_q1[(size_t)q * nE + e] = ps[kWin + t1lo + q];
+            for (int q = 0; q < nq; q++)
+                q1[(size_t)q * nE + e] = (Wt)(q < cnt ? ps[kWin + t1lo + q] : 0.0);
         }
+    });
     // ---- adjoint lists: tiles of R x BCa grid points (one per warp lane);
     // per tile the nodes whose window meets it, ascending.  Tiles are
     // numbered block-major: tile = b * nbands + v.
     const int nblka = L->nblka;
-    std::vector<int> bstamp(nblka, -1), vstamp(nb, -1);
-    int blks[16], bands[16];
-    auto visit = [&](int j, auto &&fn) {
-        int nbk = 0, nbd = 0;
+    // the blocks and bands met by node j's window (each once)
+    auto visit = [&](int j, std::vector<int> &bstamp, std::vector<int> &vstamp, auto &&fn) {
+        int blks[16], bands[16], nbk = 0, nbd = 0;
         for (int s = 0; s < kWin; s++) {
             int b = ((t.u1[j] + s) & (n1 - 1)) / BCa;
             int v = ((t.u0[j] + s) & (n0 - 1)) / R;
@@ -364,34 +396,54 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
             for (int c = 0; c < nbd; c++) fn((size_t)blks[a] * nb + bands[c]);
     };
     size_t ntiles = (size_t)nblka * nb;
+    // counts per (node range, tile), node ranges in ascending order; a
+    // tile's entries of range k follow those of range k - 1, so every list
+    // stays in ascending node order
+    const int kParts = 16;
+    std::vector<std::vector<int>> pc(kParts);
+    int nparts = parallel_for(M, 4096, [&](int j0, int j1, int k) {
+        std::vector<int> bs(nblka, -1), vs(nb, -1);
+        pc[k].assign(ntiles, 0);
+        for (int j = j0; j < j1; j++) visit(j, bs, vs, [&](size_t tile) { pc[k][tile]++; });
+    });
     std::vector<int> cnt(ntiles + 1, 0);
-    for (int j = 0; j < M; j++) visit(j, [&](size_t tile) { cnt[tile + 1]++; });
-    for (size_t i = 0; i < ntiles; i++) cnt[i + 1] += cnt[i];
+    for (size_t i = 0; i < ntiles; i++) {
+        int sum = 0;
+        for (int k = 0; k < nparts; k++) sum += pc[k][i];
+        cnt[i + 1] = cnt[i] + sum;
+    }
     L->band_off = cnt;
     L->band_node.assign(cnt[ntiles], 0);
     // per entry the tile's window weights: R row weights psi0(v*R + rr - u0)
     // then BCa column weights psi1(b*BCa + cc - u1), zero outside the window
     const int W = R + BCa;
-    L->band_w.assign((size_t)cnt[ntiles] * W, 0.0);
-    std::vector<int> pos(cnt.begin(), cnt.end() - 1);
-    std::fill(bstamp.begin(), bstamp.end(), -1);
-    std::fill(vstamp.begin(), vstamp.end(), -1);
-    for (int j = 0; j < M; j++)
-        visit(j, [&](size_t tile) {
-            int e = pos[tile]++;
-            L->band_node[e] = j;
-            int b = (int)(tile / nb), v = (int)(tile % nb);
-            double *w = &L->band_w[(size_t)e * W];
-            const double *ps = &t.psi[(size_t)j * 2 * kWin];
-            for (int rr = 0; rr < R; rr++) {
-                int d = (v * R + rr - t.u0[j]) & (n0 - 1);
-                if (d < kWin) w[rr] = ps[d];
-            }
-            for (int cc = 0; cc < BCa; cc++) {
-                int d = (b * BCa + cc - t.u1[j]) & (n1 - 1);
-                if (d < kWin) w[R + cc] = ps[kWin + d];
-            }
-        });
+    L->band_w.alloc((size_t)cnt[ntiles] * W);
+    parallel_for(M, 4096, [&](int j0, int j1, int k) {
+        // first slot of this node range in every tile
+        std::vector<int> pos(ntiles);
+        for (size_t i = 0; i < ntiles; i++) {
+            int off = cnt[i];
+            for (int q = 0; q < k; q++) off += pc[q][i];
+            pos[i] = off;
+        }
+        std::vector<int> bs(nblka, -1), vs(nb, -1);
+        for (int j = j0; j < j1; j++)
+            visit(j, bs, vs, [&](size_t tile) {
+                int e = pos[tile]++;
+                L->band_node[e] = j;
+                int b = (int)(tile / nb), v = (int)(tile % nb);
+                Wt *w = L->band_w.data() + (size_t)e * W;
+                const double *ps = &t.psi[(size_t)j * 2 * kWin];
+                for (int rr = 0; rr < R; rr++) {
+                    int d = (v * R + rr - t.u0[j]) & (n0 - 1);
+                    w[rr] = (Wt)(d < kWin ? ps[d] : 0.0);
+                }
+                for (int cc = 0; cc < BCa; cc++) {
+                    int d = (b * BCa + cc - t.u1[j]) & (n1 - 1);
+                    w[R + cc] = (Wt)(d < kWin ? ps[kWin + d] : 0.0);
+                }
+            });
+    });
     // per block, its tiles longest list first (the spreading CTA hands
     // them out in this order)
     L->band_ord.resize(ntiles);
@@ -405,5 +457,8 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
     }
     return 0;
 }
+
+template int build_fused_lists<float>(const NfftTables &, int, int, bool, FusedLists<float> *);
+template int build_fused_lists<double>(const NfftTables &, int, int, bool, FusedLists<double> *);
 
 }  // namespace nudim

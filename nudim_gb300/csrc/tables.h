@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 namespace nudim {
@@ -27,10 +28,8 @@ struct NfftTables {
     std::vector<int> u0, u1;          // first window index per node (may be < 0)
     std::vector<double> psi;          // M x (2*kW): psi0[0..kW), psi1[0..kW)
     std::vector<double> c0, c1;       // 1 / (n * phi_hat(k)), centred k
-    // spreading (adjoint) tile lists: node ids whose window touches each
-    // ty x tx tile of the n0 x n1 grid, ascending, CSR layout.
+    // tiles of the grid path's spreading gather (lists: build_tile_lists)
     int ty = 16, tx = 16, nty = 0, ntx = 0;
-    std::vector<int> tile_off, tile_nodes;
 };
 
 int build_nfft_tables(int N0, int N1, int M, const double *x, int ty, int tx, NfftTables *t);
@@ -42,7 +41,17 @@ int build_nfft_tables(int N0, int N1, int M, const double *x, int ty, int tx, Nf
 //   adjoint: column blocks of BCa columns; per tile of R = 32 / BCa rows x
 //            BCa columns (one grid point per warp lane), the nodes whose
 //            window meets the tile, ascending.
-struct FusedLists {
+template <typename W> struct HostArray {  // uninitialised until written
+    std::unique_ptr<W[]> p;
+    size_t n = 0;
+    void alloc(size_t k) { p.reset(new W[k ? k : 1]); n = k; }
+    W *data() { return p.get(); }
+    const W *data() const { return p.get(); }
+    size_t size() const { return n; }
+};
+
+// W: the element type of the weights (the plan's precision).
+template <typename W> struct FusedLists {
     int BC = 0, nblk = 0, smax = 0;
     int BCa = 0, nblka = 0, R = 0, nbands = 0;
     std::vector<int> blk_off, ent;          // ent = node * 8 + slot
@@ -51,16 +60,21 @@ struct FusedLists {
     // window row, cl0 | cnt << 8, 16 aligned row weights, nq column weights
     int nq = 0;
     std::vector<int> ent_rb, ent_cc;
-    std::vector<double> ent_qa, ent_q1;
+    HostArray<W> ent_qa, ent_q1;
     std::vector<int> band_off, band_node;   // CSR over tiles b * nbands + v
-    std::vector<double> band_w;             // per entry R row + BCa column weights
+    HostArray<W> band_w;                    // per entry R row + BCa column weights
     std::vector<int> band_ord;              // per block its tiles, longest list first
 };
 
 // BC a power of two dividing n1; BCa a power of two <= 32 dividing n1.
 // Returns 0, -1 (bad shape) or -2 (a window meets one trafo block twice:
 // the grid is too narrow for column blocks of BC).
-int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists *L);
+template <typename W>
+int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists<W> *L);
+
+// Spreading tile lists of the grid path: node ids whose window touches each
+// ty x tx tile of the n0 x n1 grid, ascending, CSR layout.
+void build_tile_lists(const NfftTables &t, std::vector<int> *off, std::vector<int> *nodes);
 
 // e^{-2 pi i k / n}, k < n, interleaved (re, im)
 void fft_twiddles(int n, std::vector<double> *tw);
