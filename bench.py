@@ -195,12 +195,14 @@ def timed_steps(ctx, job, steps, nvtx=None):
 
 
 # DRAM traffic over algorithmic bytes of one launch, from one ncu capture of a
-# 20-plane launch of the same kernel on the same geometry (profiles/*_cfg2_20planes.md):
-# dram__bytes_read.sum + dram__bytes_write.sum divided by the profiler's algorithmic
-# bytes for that launch.  Traffic grows in proportion to the planes of a launch.
+# 32-plane launch of the same kernel on the same geometry
+# (profiles/spread_colifft_cfg2_32planes.md, colfft_interp_cfg2_32planes.md):
+# dram__bytes_read.sum + dram__bytes_write.sum divided by the profiler's
+# algorithmic bytes for that launch.  Both grow in proportion to the planes of a
+# launch (the node tables are the only fixed part, 6% of a 32-plane launch).
 MEASURED_TRAFFIC_RATIO = {
-    "spread": (58.727936e6 + 34.508544e6) / (69504 * 120 + 20 * 8 * (69504 + 384 * 1024)),
-    "interp": (84.525312e6 + 14.749440e6) / (69504 * 120 + 20 * 8 * (384 * 1024 + 3 * 69504)),
+    "spread": (77.462016e6 + 71.540736e6) / (69504 * 120 + 32 * 8 * (69504 + 384 * 1024)),
+    "interp": (128.151296e6 + 34.670592e6) / (69504 * 120 + 32 * 8 * (384 * 1024 + 3 * 69504)),
 }
 
 
