@@ -18,6 +18,7 @@
 //
 // No atomics: every output element has exactly one writer, and every sum
 // has a fixed order, so results are deterministic.
+#include <cstdlib>
 #include <type_traits>
 
 #include "engine.cuh"
@@ -239,7 +240,7 @@ k_rowfft(const void *__restrict__ src, size_t src_stride, int N0, int N1, int n1
 // ================================================================ K2 column pass + interpolation
 // warps per trafo column-block CTA (register room for the radix-16 FFT passes
 // and the row weights)
-template <typename T> __host__ __device__ constexpr int col_warps() { return sizeof(T) == 4 ? 16 : 8; }
+template <typename T> __host__ __device__ constexpr int col_warps() { return 8; }
 
 // Shared memory: two BC x n0 complex buffers (FFT).  After the column FFTs
 // each lane takes one (node, block) entry of the block's list and sums the
@@ -250,8 +251,11 @@ template <typename T> __host__ __device__ constexpr int col_warps() { return siz
 // pairs (FP32) against 16 row weights pre-shifted to the even first row.
 // The list holds entries with equal cnt side by side, so the lanes of a
 // warp run loops of equal length.
+#ifndef NUDIM_COL_MINB
+#define NUDIM_COL_MINB 3  // FP32 CTAs per SM the register allocation aims for
+#endif
 template <typename T>
-__global__ void __launch_bounds__(32 * col_warps<T>(), 1)
+__global__ void __launch_bounds__(32 * col_warps<T>(), sizeof(T) == 4 ? NUDIM_COL_MINB : 1)
 k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int n1, int BC,
                 const cplx_t<T> *__restrict__ tw0, const int *__restrict__ blk_off,
                 const int *__restrict__ ent, const int *__restrict__ e_rb,
@@ -518,26 +522,33 @@ k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
         T br[P], bi[P];
 #pragma unroll
         for (int p = 0; p < P; p++) br[p] = bi[p] = T(0);
+        // nodes k0 .. k0 + K of the batch (weights past the list end are zero)
+        auto nodes = [&](auto kcount) {
+            constexpr int K = decltype(kcount)::value;
 #pragma unroll
-        for (int k = 0; k < NB; k++) {
-            T q0 = wc[k * W + rr], q1 = wc[k * W + R + cc];
-            if (sizeof(T) == 4) {
-                T q = q0 * q1;
+            for (int k = 0; k < K; k++) {
+                T q0 = wc[k * W + rr], q1 = wc[k * W + R + cc];
+                if (sizeof(T) == 4) {
+                    T q = q0 * q1;
 #pragma unroll
-                for (int p = 0; p < P; p++) {
-                    C fv = fs[p * NB + k];
-                    br[p] += q * fv.x;
-                    bi[p] += q * fv.y;
-                }
-            } else {
+                    for (int p = 0; p < P; p++) {
+                        C fv = fs[p * NB + k];
+                        br[p] += q * fv.x;
+                        bi[p] += q * fv.y;
+                    }
+                } else {
 #pragma unroll
-                for (int p = 0; p < P; p++) {
-                    C fv = fs[p * NB + k];
-                    ar[p] += q1 * (q0 * fv.x);
-                    ai[p] += q1 * (q0 * fv.y);
+                    for (int p = 0; p < P; p++) {
+                        C fv = fs[p * NB + k];
+                        ar[p] += q1 * (q0 * fv.x);
+                        ai[p] += q1 * (q0 * fv.y);
+                    }
                 }
             }
-        }
+        };
+        // a short batch (the tail of most lists) runs the half-length loop
+        if (n <= NB / 2) nodes(std::integral_constant<int, NB / 2>());
+        else nodes(std::integral_constant<int, NB>());
         if (sizeof(T) == 4) {
 #pragma unroll
             for (int p = 0; p < P; p++) {
@@ -627,10 +638,17 @@ static int ilog2(int n)
 
 template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream_t st)
 {
-    // column-block width: two BC x n0 complex buffers within 128 KB
+    // column-block width: two BC x n0 complex buffers within 128 KB, at most
+    // 4 columns (measured: two 4-column CTAs per SM beat one 8-column CTA)
     int bc = (int)((128 << 10) / (2 * sizeof(C) * (size_t)t.n0));
-    if (bc > 32) bc = 32;
+    if (bc > 4) bc = 4;
     if (bc > t.n1) bc = t.n1;
+    // NUDIM_TUNE_BC caps the width (a tuning knob: narrower blocks fit more
+    // CTAs per SM at the cost of more (node, block) entries)
+    if (const char *e = getenv("NUDIM_TUNE_BC")) {
+        int v = atoi(e);
+        if (v >= 1 && v < bc) bc = v;
+    }
     int p = 1;
     while (p * 2 <= bc) p *= 2;
     bc = p;
@@ -789,7 +807,9 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
         {
             ProfScope ps(ctx, PK_INTERP, st,
                          tab + nb * c * ((double)N0 * n1 + (double)smax * M));
-            k_colfft_interp<T><<<dim3(nblk, nb), 32 * col_warps<T>(), smem_col, st>>>(
+            // one radix-16 butterfly per thread: 64 threads per column
+            const int thr = std::min(32 * col_warps<T>(), std::max(64, 64 * BC));
+            k_colfft_interp<T><<<dim3(nblk, nb), thr, smem_col, st>>>(
                 H, N0, n0, logn0, n1, BC, tw0, blk_off, ent, e_rb, e_cc, e_qa, e_q1, nE, M, smax, P);
             NUDIM_LAUNCH_CHECK();
         }
