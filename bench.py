@@ -194,33 +194,41 @@ def timed_steps(ctx, job, steps, nvtx=None):
     return e0.elapsed_time(e1)
 
 
-# DRAM traffic over algorithmic bytes of one launch, from one ncu capture of a
-# 32-plane launch of the same kernel on the same geometry
-# (profiles/spread_colifft_cfg2_32planes.md, colfft_interp_cfg2_32planes.md):
-# dram__bytes_read.sum + dram__bytes_write.sum divided by the profiler's
-# algorithmic bytes for that launch.  Both grow in proportion to the planes of a
-# launch (the node tables are the only fixed part, 6% of a 32-plane launch).
-MEASURED_TRAFFIC_RATIO = {
-    "spread": (77.462016e6 + 71.540736e6) / (69504 * 120 + 32 * 8 * (69504 + 384 * 1024)),
-    "interp": (128.151296e6 + 34.670592e6) / (69504 * 120 + 32 * 8 * (384 * 1024 + 3 * 69504)),
-}
+# DRAM bytes per Z-plane of the adjoint NFFT's two kernels, from ncu captures of
+# 32-plane launches on the same geometry (profiles/spread_colifft_cfg2_32planes.md,
+# row_passes_cfg2_32planes.md): dram__bytes_read.sum + dram__bytes_write.sum / 32.
+MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((77.462016e6 + 71.540736e6)      # k_spread_colifft
+                                      + (100.737792e6 + 36.037120e6)) / 32  # k_rowifft_crop
 
 
-def roofline_from_profile(prof, peak_gbs, peak_kind):
-    mine = {k: v for k, v in prof.items() if k not in ("fft2d", "zfft") and v[1] > 0}
+def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):
+    """Roofline of the dominant kernel pair, the adjoint NFFT (k_spread_colifft +
+    k_rowifft_crop).  Its unit is one Z-plane's adjoint NFFT, whose algorithmic bytes
+    are those of the unfused NFFT: c (P^2 + 4 n^2 + M) -- coefficients, the n x n
+    oversampled grid written, transformed (read + write) and read back, and the node
+    values.  achieved = units x that / the two kernels' measured time."""
     total = sum(v[0] for v in prof.values())
-    top = max(mine, key=lambda k: mine[k][0])
-    ms, n, b = mine[top]
-    per_launch_s = ms / n / 1e3
-    achieved = (b / n) / per_launch_s / 1e9
     shares = {k: round(v[0] / total, 4) for k, v in prof.items() if v[1] > 0}
-    ratio = MEASURED_TRAFFIC_RATIO.get(top)
-    return top, {
-        "bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak_gbs,
-        "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
-        "traffic": round(ratio * b / n) if ratio else None,
-        "algorithmic_bytes_per_launch": b / n, "avg_launch_ms": ms / n,
-        "peak_source": peak_kind}, shares
+    P, nz = r["np"], r["nz"]
+    n = 2 * (1 << (P - 1).bit_length())
+    M = 181 * P
+    unit = csize * (P * P + 4 * n * n + M)
+    ms_s, n_s, _ = prof["spread"]
+    ms_c, n_c, _ = prof["crop"]
+    # 11 adjoint NFFTs of every Z-plane per outer iteration (CGNR: one before
+    # the loop, one per step)
+    units = 11 * nz * steps
+    planes_per_launch = units / max(1, n_s)
+    secs = (ms_s + ms_c) / 1e3
+    achieved = units * unit / secs / 1e9
+    return "adjoint NFFT", {
+        "bound": "hbm", "kernel": "adjoint NFFT (k_spread_colifft + k_rowifft_crop)",
+        "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
+        "frac": round(achieved / peak_gbs, 4),
+        "traffic": round(MEASURED_ADJOINT_TRAFFIC_PER_PLANE * planes_per_launch),
+        "algorithmic_bytes_per_launch": unit * planes_per_launch,
+        "algorithmic_bytes_per_unit": unit, "units_per_launch": planes_per_launch,
+        "avg_launch_ms": (ms_s + ms_c) / n_s, "peak_source": peak_kind}, shares
 
 
 def cpu_baseline_sample(proj, r, iters=1, threads=None):
@@ -393,7 +401,9 @@ def run_ours(args):
     # ---- mixed form, device resident (the headline `value`)
     job = ng.Job(ctx, **job_kwargs(r, ng.MIXED))
     job.set_projections(proj)
-    job.step(args.warmup)
+    job.step(1)
+    vol_mixed_1 = job.volume()
+    job.step(args.warmup - 1)
     ctx.sync()
     vol_mixed_w = job.volume()
     barrier(dist)
@@ -414,7 +424,8 @@ def run_ours(args):
         ms_prof = timed_steps(ctx, job, prof_steps, "profiled")
         prof = ctx.profile_read()
         ctx.profile(False)
-        top, roof, shares = roofline_from_profile(prof, peaks.get("hbm_gbs", 6800.0), peak_kind)
+        top, roof, shares = roofline_from_profile(prof, peaks.get("hbm_gbs", 6800.0), peak_kind,
+                                                  r, 8, prof_steps)
         roof["profiled_ms_per_step"] = ms_prof / prof_steps
         log("profiled pass: top kernel %s, %.1f%% of measured HBM" % (top, 100 * roof["frac"]))
     else:
@@ -441,12 +452,14 @@ def run_ours(args):
         log("e2e: %.3e voxel-iters/s" % e2e["value"])
 
     # ---- FP64 plain form on the same job (fewer steps: it is the slow form)
-    v64 = ms64 = err = None
+    v64 = ms64 = err = err1 = None
     fp64_steps = max(1, args.fp64_steps)
     if not args.no_fp64:
         job = ng.Job(ctx, **job_kwargs(r, ng.FP64))
         job.set_projections(proj)
-        job.step(args.warmup)
+        job.step(1)
+        vol64_1 = job.volume()
+        job.step(args.warmup - 1)
         ctx.sync()
         vol64_w = job.volume()
         ms64 = timed_steps(ctx, job, fp64_steps)
@@ -454,6 +467,7 @@ def run_ours(args):
         ms64 = max_over_ranks(dist, ms64, dev)
         v64 = ws * V * fp64_steps / (ms64 / 1e3)
         err = float(np.linalg.norm(vol_mixed_w - vol64_w) / np.linalg.norm(vol64_w))
+        err1 = float(np.linalg.norm(vol_mixed_1 - vol64_1) / np.linalg.norm(vol64_1))
         log("fp64: %.2f ms/iteration, mixed vs fp64 rel L2 %.2e" % (ms64 / fp64_steps, err))
 
     line = {
@@ -471,6 +485,7 @@ def run_ours(args):
         line["fp64_plain"] = {"value": v64, "unit": "voxel-iters/s",
                               "ms_per_step": ms64 / fp64_steps, "steps": fp64_steps}
         line["mixed_over_fp64"] = value / v64
+        line["rel_l2_mixed_vs_fp64_after_1_iteration"] = err1
         line["rel_l2_mixed_vs_fp64_after_warmup"] = err
     if args.serve_jobs > 0:
         line["serving"] = {"mixed": serving_bench(ctx, args.serve_jobs, args.serve_rate, ng.MIXED)}
