@@ -130,6 +130,14 @@ __device__ __forceinline__ T diff_cell(T cv, T nN, T nS, T nE, T nW, T lambda, T
     T gN = rn_sub(nN, cv), gS = rn_sub(nS, cv), gE = rn_sub(nE, cv), gW = rn_sub(nW, cv);
     T cN = diff_coef(gN, Ksq), cS = diff_coef(gS, Ksq), cE = diff_coef(gE, Ksq),
       cW = diff_coef(gW, Ksq);
+    if (sizeof(T) == 4) {
+        // FP32 form: the same sum with fused multiply-adds
+        T sum = cN * gN;
+        sum = fma(cS, gS, sum);
+        sum = fma(cE, gE, sum);
+        sum = fma(cW, gW, sum);
+        return fma(lambda, sum, cv);
+    }
     T sum = rn_add(rn_add(rn_add(rn_mul(cN, gN), rn_mul(cS, gS)), rn_mul(cE, gE)),
                    rn_mul(cW, gW));
     return rn_add(cv, rn_mul(lambda, sum));
@@ -180,8 +188,12 @@ k_diffusion(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, int ni
 // position y - y0(d)).  During step t diagonal t + 2 is fetched into
 // registers (its slot held diagonal t + 2 - R, written back at step t - 1)
 // and diagonal t - 2G + 1, final for the group, is written back: one barrier
-// per step.  Requires min(ny, nx) <= kDiffPf * blockDim.x.
+// per step.  The cells of a step are dealt out as 64-cell segments of the
+// active diagonals, one warp per segment, from a task table (segment prefix
+// counts and ring slots) that warp 0 builds for step t + 1 during step t.
+// Requires min(ny, nx) <= kDiffPf * blockDim.x.
 constexpr int kDiffPf = 4;
+constexpr int kDiffMaxG = 64;  // sweeps per group (task tables in shared memory)
 
 template <typename T>
 __global__ void __launch_bounds__(1024)
@@ -193,10 +205,46 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
     T *U = u + (size_t)blockIdx.x * ny * nx;
     const T lambda = (T)lambda_d, Ksq = (T)ksq_d;
     const int D = ny + nx - 1, L = min(ny, nx);
-    const int P = min((int)blockDim.x, (L + 31) & ~31), gs = blockDim.x / P;
-    const int gi = threadIdx.x / P, i0 = threadIdx.x - gi * P;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    // per step (double-buffered), for active diagonal k (sweep g_lo + k):
+    // prefix count of its 64-cell tasks, d, y0(d), len(d), and the ring offsets
+    // of diagonals d, d - 1, d + 1
+    constexpr int TC = 64;
+    __shared__ int s_pre[2][kDiffMaxG + 1], s_meta[2][2];
+    __shared__ int4 s_dg[2][kDiffMaxG];   // d, y0, len, ring offset of d
+    __shared__ int2 s_nb[2][kDiffMaxG];   // ring offsets of d - 1 (d itself when d == 0) and d + 1
     auto y0 = [&](int d) { return max(0, d - (nx - 1)); };
     auto len = [&](int d) { return min(d, ny - 1) - y0(d) + 1; };
+    // warp 0: the task table of step t of a group of gc sweeps into buffer b
+    auto build_table = [&](int t, int gc, int b) {
+        const int g_hi = min(gc - 1, t / 2), a = t - (D - 1);
+        const int g_lo = a > 0 ? (a + 1) / 2 : 0, nact = g_hi - g_lo + 1;
+        int carry = 0;
+        for (int base = 0; base < nact; base += 32) {
+            const int k = base + lane;
+            int c = 0;
+            if (k < nact) {
+                const int d = t - 2 * (g_lo + k), nd = len(d), sd = d % R;
+                c = (nd + TC - 1) / TC;
+                s_dg[b][k] = make_int4(d, y0(d), nd, sd * L);
+                s_nb[b][k] = make_int2(d > 0 ? (sd == 0 ? R - 1 : sd - 1) * L : sd * L,
+                                       (sd == R - 1 ? 0 : sd + 1) * L);
+            }
+            int incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (k < nact) s_pre[b][k + 1] = carry + incl;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) {
+            s_pre[b][0] = 0;
+            s_meta[b][0] = nact;
+            s_meta[b][1] = g_lo;
+        }
+    };
     auto slot = [&](int d) { return ring + (size_t)(d % R) * L; };
     auto cell = [&](int d, int i) -> size_t {
         int a = y0(d);
@@ -209,6 +257,7 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
             T *s = slot(d);
             for (int i = threadIdx.x; i < len(d); i += blockDim.x) s[i] = U[cell(d, i)];
         }
+        if (warp == 0) build_table(0, gc, 0);
         __syncthreads();
         for (int t = 0; t < nsteps; t++) {
             // fetch diagonal t + 2
@@ -220,22 +269,54 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
                 int i = threadIdx.x + k * blockDim.x;
                 pf[k] = i < nn ? U[cell(dn, i)] : T(0);
             }
-            int g_hi = min(gc - 1, t / 2);
-            int a = t - (D - 1);
-            int g_lo = a > 0 ? (a + 1) / 2 : 0;
-            // P threads per diagonal, gs diagonals at a time; the ring slot of
-            // diagonal d = t - 2g moves down by 2 gs per g (no division)
-            if (gi < gs && g_lo + gi <= g_hi) {
-                int sd = (t - 2 * (g_lo + gi)) % R;
-                for (int g = g_lo + gi; g <= g_hi; g += gs) {
-                    const int d = t - 2 * g;
-                    const int yd = y0(d), nd = min(d, ny - 1) - yd + 1;
-                    if (i0 < nd) {
-                        T *sc = ring + (size_t)sd * L;
-                        const T *sm = d > 0 ? ring + (size_t)(sd == 0 ? R - 1 : sd - 1) * L : sc;
-                        const T *sp = ring + (size_t)(sd == R - 1 ? 0 : sd + 1) * L;
-                        const int ym = y0(d > 0 ? d - 1 : d), yp = y0(d + 1);
-                        for (int i = i0; i < nd; i += P) {
+            // the next step's task table (warp 0), then this step's tasks:
+            // 64-cell segments of the active diagonals, dealt out to the warps
+            const int tb = t & 1;
+            if (warp == 0 && t + 1 < nsteps) build_table(t + 1, gc, tb ^ 1);
+            {
+                const int *pre = s_pre[tb];
+                const int nact = s_meta[tb][0], ntask = pre[nact];
+                // this warp's contiguous share of the tasks; k: the diagonal of
+                // the first one (binary search over the prefix counts)
+                const int t_beg = (int)((long)ntask * warp / nwarps);
+                const int t_end = (int)((long)ntask * (warp + 1) / nwarps);
+                int k = 0;
+                for (int lo = 0, hi = nact - 1; lo <= hi;) {
+                    int mid = (lo + hi) >> 1;
+                    if (pre[mid + 1] <= t_beg) lo = mid + 1, k = lo;
+                    else hi = mid - 1;
+                }
+                for (int task = t_beg; task < t_end; task++) {
+                    while (pre[k + 1] <= task) k++;
+                    const int4 dg = s_dg[tb][k];
+                    const int2 nb = s_nb[tb][k];
+                    const int d = dg.x, yd = dg.y, nd = dg.z;
+                    // rows of diagonal d's neighbours: y0(d - 1) and y0(d + 1)
+                    const int ym = d > nx - 1 ? yd - 1 : 0, yp = d + 1 > nx - 1 ? yd + 1 : 0;
+                    T *sc = ring + dg.w;
+                    const T *sm = ring + nb.x, *sp = ring + nb.y;
+                    const int i0 = (task - pre[k]) * TC;
+                    const T *mb = sm + (yd - ym), *pb = sp + (yd - yp);
+#pragma unroll
+                    for (int h = 0; h < TC / 32; h++) {
+                        const int g0 = i0 + h * 32, g1 = min(nd, g0 + 32) - 1, i = g0 + lane;
+                        // an interior group of 32 cells: each has its four plain
+                        // neighbours (y in [1, ny-2], x in [1, nx-2] and x != nxb - 1,
+                        // the column the reference clamps): cell i's N and W sit at
+                        // i - 1, i of diagonal d - 1 from yd - ym, its S and E at i + 1,
+                        // i of diagonal d + 1 from yd - yp.  Along a diagonal y grows
+                        // and x falls.
+                        const int xmax = d - yd - g0, xmin = d - yd - g1;
+                        const bool inner = g0 <= g1 && yd + g0 >= 1 && yd + g1 <= ny - 2 &&
+                                           xmin >= 1 && xmax <= nx - 2 &&
+                                           !(xmin <= nxb - 1 && nxb - 1 <= xmax);
+                        if (__all_sync(0xffffffffu, inner)) {  // warp-uniform: a real branch
+                            if (i <= g1) {
+                                T cv = sc[i];
+                                sc[i] = diff_cell<T>(cv, mb[i - 1], pb[i + 1], pb[i], mb[i], lambda,
+                                                     Ksq);
+                            }
+                        } else if (i <= g1) {
                             int y = yd + i, x = d - y;
                             T cv = sc[i];
                             T nN = cv, nS = cv, nW = cv, nE = cv;
@@ -247,8 +328,6 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
                             sc[i] = diff_cell<T>(cv, nN, nS, nE, nW, lambda, Ksq);
                         }
                     }
-                    sd -= 2 * gs;
-                    if (sd < 0) sd += R;
                 }
             }
             if (nn > 0) {
@@ -286,9 +365,10 @@ int diffusion_run(T *u, int nz, int ny, int nx, int nx_bound, float lambda, floa
     // SM; otherwise one CTA of 1024 threads with up to 160 KB of ring
     bool two = sizeof(T) == 4 && P <= 512;
     int threads = two ? 2 * P : 1024;
-    const size_t budget = two ? ((size_t)110 << 10) : ((size_t)160 << 10);
+    const size_t budget = two ? ((size_t)108 << 10) : ((size_t)160 << 10);
     int G = (int)((budget / (sizeof(T) * (size_t)L) - 2) / 2);
     if (G > niter) G = niter;
+    if (G > kDiffMaxG) G = kDiffMaxG;
     if (G >= 1 && L <= kDiffPf * threads) {
         int R = 2 * G + 2;
         size_t smem = sizeof(T) * (size_t)R * L;
