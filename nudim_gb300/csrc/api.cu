@@ -475,11 +475,12 @@ static size_t job_bytes(const nudim_job_desc *d, int A, bool both, size_t fused_
         size_t b = 2 * V * sT + 3 * V * sC + 4 * nz * M * sC;
         if (d->denoise == NUDIM_DENOISE_TV) b += V * sT;
         b += M * (8 + 28 * sT + 20);  // node tables and tile lists
-        // fused-path lists: ~11 adjoint tile entries and <= 3 trafo entries per node
-        b += M * (11 * (4 + 12 * sT) + 3 * (8 + 24 * sT));
+        // fused-path lists: ~11 adjoint tile entries and <= 5 trafo entries per
+        // node (4-column blocks): id + 12 weights, and 3 ints + 20 weights
+        b += M * (11 * (4 + 12 * sT) + 5 * (12 + 20 * sT));
         b += nz * (size_t)cgnr_part_stride((int)M, (int)P2) * 8;
         // fused-path workspace: row spectra + partials of one chunk of planes
-        size_t plane = (np * n1 + 3 * M) * sC, chunk = fused_budget / plane;
+        size_t plane = (np * n1 + 5 * M) * sC, chunk = fused_budget / plane;
         b += (chunk < 1 ? 1 : chunk < nz ? chunk : nz) * plane;
         return b;
     };

@@ -686,7 +686,12 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
                   : p == 2 ? spread_stage_bytes<T, 2>(Wa) : spread_stage_bytes<T, 1>(Wa);
         return (p + 1) * bufa + kSpreadWarps * st;
     };
+    // NUDIM_TUNE_PLANES caps the planes per CTA (a tuning knob)
     Pa = 4;
+    if (const char *e = getenv("NUDIM_TUNE_PLANES")) {
+        int v = atoi(e);
+        if (v >= 1 && v < 4) Pa = v >= 2 ? 2 : 1;
+    }
     while (Pa > 1 && spread_smem(Pa) > ((size_t)212 << 10)) Pa /= 2;
     smem_spread = spread_smem(Pa);
     // The limit is a property of the kernel, shared by every plan in the
