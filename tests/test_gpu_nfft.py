@@ -47,25 +47,29 @@ def test_trafo_adjoint_vs_oracle(gpu_ctx, orc, nudim_built, N0, N1, kind, prec):
     plan.close()
 
 
-@pytest.mark.parametrize("P,nz", [(128, 2), (384, 1)])
-def test_trafo_adjoint_benchmark_plane_sizes(gpu_ctx, orc, nudim_built, P, nz):
-    """One or two planes at the P of the benchmark configurations."""
+@pytest.mark.parametrize("P,nz,prec", [(128, 2, 0), (384, 1, 0), (512, 1, 0), (768, 1, 0),
+                                       (768, 2, 1)])
+def test_trafo_adjoint_benchmark_plane_sizes(gpu_ctx, orc, nudim_built, P, nz, prec):
+    """Planes at the P of the benchmark configurations (cfg1 128, cfg2 384,
+    cfg5 768: a 2048-point grid, one plane per spreading CTA, 3 rows per row
+    pass) and between."""
     import torch
     rng = np.random.default_rng(P)
-    x = orc.polar_nodes(-60, 60, 3 if P == 128 else 2, 1, P)
-    plan = nudim_built.NfftPlan(gpu_ctx, P, P, x, 0)
+    x = orc.polar_nodes(-60, 60, {128: 3, 768: 1}.get(P, 2), 1, P)
+    plan = nudim_built.NfftPlan(gpu_ctx, P, P, x, prec)
     ref = orc.NFFT(P, P, x)
     fh = rng.standard_normal((nz, P, P)) + 1j * rng.standard_normal((nz, P, P))
     y = rng.standard_normal((nz, len(x))) + 1j * rng.standard_normal((nz, len(x)))
-    fh_d, y_d = to_dev(fh, np.complex128), to_dev(y, np.complex128)
-    f_d = torch.zeros((nz, len(x)), dtype=torch.complex128, device="cuda")
-    g_d = torch.zeros((nz, P, P), dtype=torch.complex128, device="cuda")
+    fh_d, y_d = to_dev(fh, cdtype(prec)), to_dev(y, cdtype(prec))
+    f_d = torch.zeros((nz, len(x)), dtype=fh_d.dtype, device="cuda")
+    g_d = torch.zeros((nz, P, P), dtype=fh_d.dtype, device="cuda")
     plan.trafo(nz, fh_d.data_ptr(), f_d.data_ptr())
     plan.adjoint(nz, y_d.data_ptr(), g_d.data_ptr())
     torch.cuda.synchronize()
+    tol = 1e-10 if prec == 0 else 2e-5
     for b in range(nz):
-        assert rel(f_d[b].cpu().numpy(), ref.trafo(fh[b])) < 1e-10
-        assert rel(g_d[b].cpu().numpy(), ref.adjoint(y[b])) < 1e-10
+        assert rel(f_d[b].cpu().numpy(), ref.trafo(fh[b])) < tol
+        assert rel(g_d[b].cpu().numpy(), ref.adjoint(y[b])) < tol
 
 
 @pytest.mark.parametrize("weighted,prec", [(True, 0), (False, 0), (True, 1)])
