@@ -91,7 +91,7 @@ def build(verbose=False, force=False):
         if force or _stale(exe, paths + [LIB, os.path.join(INC, "nudim.h")]):
             variant = "1" if name.endswith("_parallel") else "0"
             _run(["gcc", "-O2", "-std=gnu99", "-DNUDIM_CLI_VARIANT=" + variant, "-I", INC,
-                  *paths, "-o", exe, "-L" + PKG, "-lnudim", "-Wl,-rpath,$ORIGIN/..", "-lm"])
+                  *paths, "-o", exe, "-L" + PKG, "-lnudim", "-Wl,-rpath,$ORIGIN/..", "-lm", "-pthread"])
     return LIB
 
 
