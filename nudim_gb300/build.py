@@ -28,6 +28,7 @@ CLI = {
     "reconstruction": ["cli/reconstruction.c", "cli/textio.c"],
     "reconstruction_parallel": ["cli/reconstruction.c", "cli/textio.c"],
     "projection_sim": ["cli/projection_sim.c", "cli/textio.c"],
+    "mrc2prj": ["cli/mrc2prj.c", "cli/textio.c"],
 }
 
 
