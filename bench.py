@@ -260,15 +260,15 @@ def cpu_baseline_sample(proj, r, iters=1, threads=None):
             "s_per_iter": t_iter}
 
 
-def serving_specs(n_jobs, seed):
+def serving_specs(n_jobs, seed, big_share=0.1, nhio=10, ner=10, weight=1):
     """Uneven jobs of the batched/serving configurations: nx from
     {96,128,160,192,256}, nz from 32..256 step 16, pad = round16(U(1.25,1.5)
-    * nx), symmetric max tilt U{45..70}, step {1,2,3}; one job in ten is
-    384 x 384 x 192 (pad 480..576).  20 HIO + 30 ER, TV, --weight."""
+    * nx), symmetric max tilt U{45..70}, step {1,2,3}; a `big_share` of the
+    jobs is 384 x 384 x 192 (pad 480..576).  TV denoise."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(n_jobs):
-        if rng.uniform() < 0.1:
+        if rng.uniform() < big_share:
             nx, nz = 384, 192
         else:
             nx = int(rng.choice([96, 128, 160, 192, 256]))
@@ -278,18 +278,15 @@ def serving_specs(n_jobs, seed):
         gmax = int(rng.integers(45, 71))
         gmax -= gmax % step
         out.append(dict(nx=nx, nz=nz, np=npad, gam_min=-gmax, gam_max=gmax, interval=step,
-                        padangle=1, nhio=10, ner=10, denoise=1, weight=1, seed=seed + k))
+                        padangle=1, nhio=nhio, ner=ner, denoise=1, weight=weight, seed=seed + k))
     return out
 
 
-def serving_bench(ctx, n_jobs, rate, precision, seed=20261205):
-    """Poisson arrivals at `rate` jobs/s into the continuous-batching server;
-    returns p50/p99 arrival-to-result latency and completed jobs/s."""
-    import torch
-
+def uneven_inputs(ctx, specs):
+    """Seeded blob phantoms and noisy (SNR 1) GPU-simulated tilt series for
+    `specs`; returns [(tilt series, job arguments)]."""
     import nudim_gb300 as ng
     from nudim_gb300.synth import add_noise, blob_phantom
-    specs = serving_specs(n_jobs, seed)
     inputs = []
     for sp in specs:
         s = dict(sp)
@@ -299,6 +296,74 @@ def serving_bench(ctx, n_jobs, rate, precision, seed=20261205):
                            amp_range=(0.2, 1.0), seed=sd)
         proj = ng.project_2d1d(ctx, vol, nx, s["gam_min"], s["gam_max"], s["interval"])
         inputs.append((add_noise(proj, 1.0, sd + 1), s))
+    return inputs
+
+
+def batched_bench(ctx, n_jobs, steps, warmup, precision, seed=20261206):
+    """The batched configuration: `n_jobs` independent uneven tomograms
+    (ner=30 ER iterations with TV, no HIO), all resident, stepped together
+    by nudim_step (each job's iteration is a graph replay on its own stream,
+    so small jobs overlap).  Timed: `steps` iterations of every job, host
+    clock between two device-wide synchronizations."""
+    import torch
+
+    import nudim_gb300 as ng
+    specs = serving_specs(n_jobs, seed, big_share=0.0, nhio=0, ner=30, weight=0)
+    inputs = uneven_inputs(ctx, specs)
+    t0 = time.perf_counter()
+    jobs = []
+    for proj, s in inputs:
+        jb = ng.Job(ctx, precision=precision, **s)
+        jb.set_projections(proj)
+        jobs.append(jb)
+    t_setup = time.perf_counter() - t0
+    vox = sum(s["nz"] * s["np"] ** 2 for _, s in inputs)
+    ctx.step(jobs, warmup)
+    torch.cuda.synchronize()
+    n0 = ng.lib().nudim_launch_count()
+    t0 = time.perf_counter()
+    ctx.step(jobs, steps)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    launches = int(ng.lib().nudim_launch_count() - n0)
+    shares = serial_ms = None
+    if warmup + steps < 30:
+        # one more iteration of every job, one job at a time (events around
+        # short kernels of one stream would otherwise also time the other
+        # streams' kernels), with per-kernel-class CUDA events: each class's
+        # share of the summed kernel time
+        ctx.profile(True)
+        t0 = time.perf_counter()
+        for jb in jobs:
+            ctx.step([jb], 1)
+            torch.cuda.synchronize()
+        serial_ms = 1e3 * (time.perf_counter() - t0)
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        total = sum(v[0] for v in prof.values())
+        shares = {k: round(v[0] / total, 4) for k, v in prof.items() if v[1] > 0}
+    for jb in jobs:
+        jb.close()
+    out = {"value": vox * steps / t, "unit": "voxel-iters/s", "jobs": n_jobs,
+           "voxels_total": int(vox), "steps": steps, "warmup": warmup,
+           "ms_per_step": 1e3 * t / steps, "gpu_launches": launches,
+           "setup_s": t_setup, "kernel_time_share": shares,
+           "serial_profiled_ms_per_step": serial_ms,
+           "timer": "host clock between device-wide synchronizations (one stream per job)",
+           "sizes": "nx {96..256}, nz 32..256 step 16, pad 1.25-1.5 nx, tilt +-45..70 step "
+                    "1/2/3, ner=30, TV"}
+    log("batched: %d jobs, %.1f ms/step, %.3e voxel-iters/s" % (n_jobs, out["ms_per_step"],
+                                                                  out["value"]))
+    return out
+
+
+def serving_bench(ctx, n_jobs, rate, precision, seed=20261205):
+    """Poisson arrivals at `rate` jobs/s into the continuous-batching server;
+    returns p50/p99 arrival-to-result latency and completed jobs/s."""
+    import torch
+
+    import nudim_gb300 as ng
+    inputs = uneven_inputs(ctx, serving_specs(n_jobs, seed))
     arrivals = np.cumsum(np.random.default_rng(seed + 7).exponential(1.0 / rate, n_jobs))
     free, _ = torch.cuda.mem_get_info()
     srv = ng.Server(ctx, int(0.7 * free), max_active=16)
@@ -487,6 +552,9 @@ def run_ours(args):
         line["mixed_over_fp64"] = value / v64
         line["rel_l2_mixed_vs_fp64_after_1_iteration"] = err1
         line["rel_l2_mixed_vs_fp64_after_warmup"] = err
+    if args.batch_jobs > 0:
+        line["batched"] = {"mixed": batched_bench(ctx, args.batch_jobs, args.steps, args.warmup,
+                                                  ng.MIXED)}
     if args.serve_jobs > 0:
         line["serving"] = {"mixed": serving_bench(ctx, args.serve_jobs, args.serve_rate, ng.MIXED)}
         if args.serve_fp64:
@@ -513,6 +581,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--batch-jobs", type=int, default=48,
+                    help="jobs in the batched measurement (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=16,
                     help="jobs in the serving measurement (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=0.5, help="Poisson arrivals, jobs/s")

@@ -3,7 +3,8 @@
 //
 // Arithmetic uses round-to-nearest intrinsics (no contraction) so that the
 // FP64 form reproduces the reference's per-voxel C arithmetic exactly; only
-// the two global sums of TV are summed in a different (tree) order.
+// the two global sums of TV are summed in a different (tree) order.  The
+// FP32 form uses fused multiply-adds, rsqrt and fast division where noted.
 #include "engine.cuh"
 
 namespace nudim {
@@ -11,82 +12,280 @@ namespace nudim {
 // ================================================================ TV
 // denoise.c:67-151 / 153-249 called as total_variation_discrete(img, lam,
 // niter, nz, np, np): the reference's i runs over Z, j over Y, k over X.
+//
+// One TV iteration is two launches:
+//   k_tv_grad   the gradient g of every voxel and the two global sums
+//               (sum g^2, sum of squares of the negative voxels).  A block
+//               owns a 32 x 8 (x, y) tile and a run of Z-planes; it marches
+//               along Z with three planes of the tile plus a one-cell halo in
+//               shared memory, so every voxel is read from memory about once.
+//               The halo cells hold the clamped neighbours (index -1 -> 0,
+//               n -> n-1), which are exactly the reference's boundary rules.
+//               The block that finishes last sums the per-block partials in
+//               block order (deterministic) into scal[0..1];
+//   k_tv_update u -= (lam sqrt(scal[1])) (g / sqrt(scal[0])).
+constexpr int kTvTX = 32, kTvTY = 8, kTvSX = kTvTX + 2, kTvSY = kTvTY + 2;
+
+// Gradient of voxel (i, j, k) (denoise.c:84-122) from three tile planes:
+// p = plane clamp(i-1), q = plane i, r = plane clamp(i+1), the voxel at
+// tile cell (y, x).
 template <typename T>
-__global__ void __launch_bounds__(256)
-k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part, int nz, int ny,
-          int nx, int height, int ylo, int yhi)
+__device__ __forceinline__ T tv_point(const T (*p)[kTvSX], const T (*q)[kTvSX],
+                                      const T (*r)[kTvSX], int y, int x, T &c)
 {
-    __shared__ double sh[32];
-    size_t V = (size_t)nz * ny * nx;
-    size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double sg = 0, sn = 0;
-    if (o < V) {
-        int k = (int)(o % nx);
-        size_t q = o / nx;
-        int j = (int)(q % ny);
-        int i = (int)(q / ny);
-        if (!height || (j >= ylo && j <= yhi)) {
-            int ip = (i == nz - 1) ? nz - 1 : i + 1, im = (i == 0) ? 0 : i - 1;
-            int jp = (j == ny - 1) ? ny - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
-            int kp = (k == nx - 1) ? nx - 1 : k + 1, km = (k == 0) ? 0 : k - 1;
-            auto at = [&](int a, int b, int c) { return u[((size_t)a * ny + b) * nx + c]; };
-            const T eps = (T)1e-8;
-            T c = u[o];
-            T t1 = rn_sub(c, at(im, j, k));
-            T t2 = rn_sub(c, at(i, jm, k));
-            T t3 = rn_sub(c, at(i, j, km));
-            T a4 = at(ip, j, k);
-            T t4 = rn_sub(a4, c);
-            T t5 = rn_sub(a4, at(ip, jm, k));
-            T t6 = rn_sub(a4, at(ip, j, km));
-            T a7 = at(i, jp, k);
-            T t7 = rn_sub(a7, at(im, jp, k));
-            T t8 = rn_sub(a7, c);
-            T t9 = rn_sub(a7, at(i, jp, km));
-            T a10 = at(i, j, kp);
-            T t10 = rn_sub(a10, at(im, j, kp));
-            T t11 = rn_sub(a10, at(i, jm, kp));
-            T t12 = rn_sub(a10, c);
-            auto nrm = [&](T x, T y, T z) {
-                return rn_sqrt(rn_add(rn_add(rn_add(eps, rn_mul(x, x)), rn_mul(y, y)), rn_mul(z, z)));
-            };
-            T g1 = rn_div(rn_add(rn_add(t1, t2), t3), nrm(t1, t2, t3));
-            T g2 = rn_div(t4, nrm(t4, t5, t6));
-            T g3 = rn_div(t8, nrm(t7, t8, t9));
-            T g4 = rn_div(t12, nrm(t10, t11, t12));
-            T gv = rn_sub(rn_sub(rn_sub(g1, g2), g3), g4);
-            g[o] = gv;
-            sg = (double)gv * (double)gv;
-            if (c < T(0)) sn = (double)c * (double)c;
-        }
+    const T eps = (T)1e-8;
+    c = q[y][x];
+    T t1 = rn_sub(c, p[y][x]);
+    T t2 = rn_sub(c, q[y - 1][x]);
+    T t3 = rn_sub(c, q[y][x - 1]);
+    T a4 = r[y][x];
+    T t4 = rn_sub(a4, c);
+    T t5 = rn_sub(a4, r[y - 1][x]);
+    T t6 = rn_sub(a4, r[y][x - 1]);
+    T a7 = q[y + 1][x];
+    T t7 = rn_sub(a7, p[y + 1][x]);
+    T t8 = rn_sub(a7, c);
+    T t9 = rn_sub(a7, q[y + 1][x - 1]);
+    T a10 = q[y][x + 1];
+    T t10 = rn_sub(a10, p[y][x + 1]);
+    T t11 = rn_sub(a10, q[y - 1][x + 1]);
+    T t12 = rn_sub(a10, c);
+    if (sizeof(T) == 4) {
+        // FP32 form: t / sqrt(eps + x^2 + y^2 + z^2) as t * rsqrt(...) with
+        // fused multiply-adds (a few ulp per term, against one for IEEE sqrt
+        // and division; the loop's own amplification of rounding dominates)
+        auto inv = [&](float x, float y, float z) {
+            return rsqrtf(fmaf(z, z, fmaf(y, y, fmaf(x, x, (float)eps))));
+        };
+        float h1 = ((float)t1 + (float)t2 + (float)t3) * inv(t1, t2, t3);
+        float h2 = (float)t4 * inv(t4, t5, t6);
+        float h3 = (float)t8 * inv(t7, t8, t9);
+        float h4 = (float)t12 * inv(t10, t11, t12);
+        return (T)(h1 - h2 - h3 - h4);
     }
-    sg = block_sum(sg, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = sg;
-    sn = block_sum(sn, sh);
-    if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = sn;
+    auto nrm = [&](T x, T y, T z) {
+        return rn_sqrt(rn_add(rn_add(rn_add(eps, rn_mul(x, x)), rn_mul(y, y)), rn_mul(z, z)));
+    };
+    T g1 = rn_div(rn_add(rn_add(t1, t2), t3), nrm(t1, t2, t3));
+    T g2 = rn_div(t4, nrm(t4, t5, t6));
+    T g3 = rn_div(t8, nrm(t7, t8, t9));
+    T g4 = rn_div(t12, nrm(t10, t11, t12));
+    return rn_sub(rn_sub(rn_sub(g1, g2), g3), g4);
 }
 
-// u -= (lam * sqrt(dA)) * (g / sqrt(sum g^2))   (denoise.c:125-142)
+// A thread's running sum of its voxels' terms: plain in the FP64 form,
+// Neumaier-compensated in the FP32 form (a thread sums one term per plane of
+// its Z-run).
+template <typename T> struct TvAcc {
+    T s = 0, e = 0;
+    __device__ __forceinline__ void add(T x)
+    {
+        if (sizeof(T) == 8) {
+            s = rn_add(s, x);
+            return;
+        }
+        T t = rn_add(s, x);
+        e = rn_add(e, fabs(s) >= fabs(x) ? rn_add(rn_sub(s, t), x) : rn_add(rn_sub(x, t), s));
+        s = t;
+    }
+    __device__ __forceinline__ T value() const { return rn_add(s, e); }
+};
+
+// The two sums: FP64 products and sums in the FP64 form; FP32 products and
+// compensated per-thread sums, FP32 warp sums and FP64 across warps and
+// blocks in the FP32 form.  Grid (x tiles, y tiles, Z-runs of zc planes);
+// 256 threads, thread (ty, tx) owns column (j0 + ty, k0 + tx).  done: a
+// zeroed counter (the last block resets it).
 template <typename T>
+__global__ void __launch_bounds__(256)
+k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part,
+          unsigned *__restrict__ done, double *__restrict__ scal, int nz, int ny, int nx,
+          int zc, int height, int ylo, int yhi)
+{
+    constexpr int kCells = kTvSY * kTvSX, kSlots = (kCells + 255) / 256;
+    __shared__ T pl[3][kTvSY][kTvSX];
+    __shared__ double sh[32];
+    __shared__ int s_last;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int k0 = blockIdx.x * kTvTX, j0 = blockIdx.y * kTvTY;
+    const int z0 = blockIdx.z * zc, z1 = min(nz, z0 + zc);
+    const int k = k0 + tx, j = j0 + ty;
+    const bool own = k < nx && j < ny && (!height || (j >= ylo && j <= yhi));
+    const size_t P = (size_t)ny * nx;
+    // this thread's halo-tile cells and their clamped in-plane offsets
+    int cell[kSlots];
+    size_t off[kSlots];
+#pragma unroll
+    for (int s = 0; s < kSlots; s++) {
+        int c = threadIdx.x + 256 * s;
+        cell[s] = c < kCells ? c : -1;
+        int yy = c / kTvSX, xx = c - yy * kTvSX;
+        int gj = min(max(j0 + yy - 1, 0), ny - 1), gk = min(max(k0 + xx - 1, 0), nx - 1);
+        off[s] = (size_t)gj * nx + gk;
+    }
+    T pre[kSlots];
+    auto fetch = [&](int plane) {
+#pragma unroll
+        for (int s = 0; s < kSlots; s++)
+            if (cell[s] >= 0) pre[s] = u[(size_t)plane * P + off[s]];
+    };
+    auto store = [&](int b) {
+#pragma unroll
+        for (int s = 0; s < kSlots; s++)
+            if (cell[s] >= 0) (&pl[b][0][0])[cell[s]] = pre[s];
+    };
+    int bp = 0, bc = 1, bn = 2;
+    fetch(max(z0 - 1, 0));
+    store(bp);
+    fetch(z0);
+    store(bc);
+    fetch(min(z0 + 1, nz - 1));
+    store(bn);
+    __syncthreads();
+    TvAcc<T> ag, an;
+    for (int i = z0; i < z1; i++) {
+        if (i + 1 < z1) fetch(min(i + 2, nz - 1));  // in flight during the compute
+        if (own) {
+            T c;
+            T gv = tv_point<T>(pl[bp], pl[bc], pl[bn], ty + 1, tx + 1, c);
+            g[(size_t)i * P + (size_t)j * nx + k] = gv;
+            ag.add(rn_mul(gv, gv));
+            if (c < T(0)) an.add(rn_mul(c, c));
+        }
+        __syncthreads();
+        if (i + 1 < z1) {
+            int t = bp;
+            bp = bc;
+            bc = bn;
+            bn = t;
+            store(bn);
+            __syncthreads();
+        }
+    }
+    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    double bg = block_sum_t<T>(ag.value(), sh);
+    double bn2 = block_sum_t<T>(an.value(), sh);
+    if (threadIdx.x == 0) {
+        part[bid] = bg;
+        part[nblk + bid] = bn2;
+        __threadfence();
+        s_last = atomicAdd(done, 1u) == nblk - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    // the last block: every block's partials are visible (fence before the
+    // count); sum them in block order, the same order whichever block is last
+    __threadfence();
+    double a = 0, b = 0;
+    for (int t = threadIdx.x; t < (int)nblk; t += blockDim.x) {
+        a += __ldcg(part + t);
+        b += __ldcg(part + nblk + t);
+    }
+    a = block_sum(a, sh);
+    b = block_sum(b, sh);
+    if (threadIdx.x == 0) {
+        scal[0] = a;
+        scal[1] = b;
+        *done = 0;
+    }
+}
+
+template <typename T, int N> struct alignas(sizeof(T) * N) TvVec {
+    T v[N];
+};
+
+// u -= (lam * sqrt(dA)) * (g / sqrt(sum g^2))   (denoise.c:125-142), VEC
+// voxels per access.  The two scalars are formed once per block (the same
+// FP64 expressions in every block, so every voxel sees the same values).
+template <typename T, typename I, int VEC>
 __global__ void __launch_bounds__(256)
 k_tv_update(T *__restrict__ u, const T *__restrict__ g, const double *__restrict__ scal,
             double lam, int nz, int ny, int nx, int height, int ylo, int yhi)
 {
-    size_t V = (size_t)nz * ny * nx;
-    size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= V) return;
-    if (height) {
-        int j = (int)((o / nx) % ny);
-        if (j < ylo || j > yhi) return;
+    __shared__ T s_tn, s_la;
+    if (threadIdx.x == 0) {
+        s_tn = (T)sqrt(scal[0]);
+        s_la = (T)(lam * sqrt(scal[1]));
     }
-    T tn = (T)sqrt(scal[0]);
-    T la = (T)(lam * sqrt(scal[1]));
-    u[o] = rn_sub(u[o], rn_mul(la, rn_div(g[o], tn)));
+    __syncthreads();
+    const T tn = s_tn, la = s_la;
+    const I nv = (I)nz * ny * nx / VEC, stride = (I)gridDim.x * blockDim.x;
+    for (I t = (I)blockIdx.x * blockDim.x + threadIdx.x; t < nv; t += stride) {
+        TvVec<T, VEC> x = reinterpret_cast<const TvVec<T, VEC> *>(u)[t];
+        const TvVec<T, VEC> y = reinterpret_cast<const TvVec<T, VEC> *>(g)[t];
+#pragma unroll
+        for (int e = 0; e < VEC; e++) {
+            if (height) {
+                int j = (int)(((t * VEC + e) / (I)nx) % (I)ny);
+                if (j < ylo || j > yhi) continue;
+            }
+            x.v[e] = rn_sub(x.v[e], rn_mul(la, rn_div(y.v[e], tn)));
+        }
+        reinterpret_cast<TvVec<T, VEC> *>(u)[t] = x;
+    }
 }
 
+// Per-block partial sums of k_tv_grad (two per block; at most one block per
+// tile and plane) and the completion counter.
 int tv_part_count(int nz, int ny, int nx)
 {
-    return 2 * ceil_div((long)nz * ny * nx, 256) + 2;
+    return 2 * ceil_div(nx, kTvTX) * ceil_div(ny, kTvTY) * nz + 2;
+}
+
+template <typename T> static int tv_grad_blocks_per_sm()
+{
+    static const int occ = [] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tv_grad<T>, 256, 0) !=
+                cudaSuccess ||
+            b < 1)
+            b = 1;
+        return b;
+    }();
+    return occ;
+}
+
+template <typename T, typename I>
+static int tv_launch(T *u, T *grad, double *part, int part_cap, double *scal, size_t V, int nz,
+                     int ny, int nx, float lam, int niter, int height, int ylo, int yhi,
+                     cudaStream_t st)
+{
+    int dev = 0, sms = 0;
+    NUDIM_CUDA(cudaGetDevice(&dev));
+    NUDIM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // Z-runs: about two resident waves of blocks, runs of at least 4 planes
+    // (each run re-reads two planes beyond its ends)
+    const long tiles = (long)ceil_div(nx, kTvTX) * ceil_div(ny, kTvTY);
+    const long want = 2L * sms * tv_grad_blocks_per_sm<T>();
+    const int runs = (int)std::max(1L, std::min((long)nz / 4, (long)ceil_div(want, tiles)));
+    const int zc = ceil_div(nz, runs);
+    const dim3 gg(ceil_div(nx, kTvTX), ceil_div(ny, kTvTY), ceil_div(nz, zc));
+    const long nb = (long)gg.x * gg.y * gg.z;
+    if (part_cap < 2 * nb + 1) {
+        set_error("tv_run: partial buffer too small");
+        return NUDIM_EINVAL;
+    }
+    unsigned *done = reinterpret_cast<unsigned *>(part + 2 * nb);
+    NUDIM_CUDA(cudaMemsetAsync(done, 0, sizeof(unsigned), st));
+    // widest access that divides the volume and both pointers' alignment
+    constexpr int W = 16 / sizeof(T);
+    const bool wide = V % W == 0 && (reinterpret_cast<uintptr_t>(u) % 16) == 0 &&
+                      (reinterpret_cast<uintptr_t>(grad) % 16) == 0;
+    const long nu = std::min((long)ceil_div((long)(wide ? V / W : V), 256), (long)sms * 8);
+    for (int it = 0; it < niter; it++) {
+        k_tv_grad<T><<<gg, 256, 0, st>>>(u, grad, part, done, scal, nz, ny, nx, zc, height, ylo,
+                                         yhi);
+        NUDIM_LAUNCH_CHECK();
+        if (wide)
+            k_tv_update<T, I, W><<<(int)nu, 256, 0, st>>>(u, grad, scal, (double)lam, nz, ny, nx,
+                                                           height, ylo, yhi);
+        else
+            k_tv_update<T, I, 1><<<(int)nu, 256, 0, st>>>(u, grad, scal, (double)lam, nz, ny, nx,
+                                                           height, ylo, yhi);
+        NUDIM_LAUNCH_CHECK();
+    }
+    return NUDIM_OK;
 }
 
 template <typename T>
@@ -94,20 +293,13 @@ int tv_run(T *u, T *grad, double *part, int part_cap, double *scal, int nz, int 
            float lam, int niter, int height, int ylo, int yhi, cudaStream_t st)
 {
     size_t V = (size_t)nz * ny * nx;
-    int nb = ceil_div((long)V, 256);
-    if (part_cap < 2 * nb) {
-        set_error("tv_run: partial buffer too small");
-        return NUDIM_EINVAL;
-    }
-    for (int it = 0; it < niter; it++) {
-        k_tv_grad<T><<<nb, 256, 0, st>>>(u, grad, part, nz, ny, nx, height, ylo, yhi);
-        NUDIM_LAUNCH_CHECK();
-        launch_finish_sums(part, nb, 1, 2 * nb, scal, 2, 2, st);
-        k_tv_update<T><<<nb, 256, 0, st>>>(u, grad, scal, (double)lam, nz, ny, nx, height, ylo,
-                                           yhi);
-        NUDIM_LAUNCH_CHECK();
-    }
-    return NUDIM_OK;
+    if (V == 0 || niter <= 0) return NUDIM_OK;
+    // 32-bit voxel indices while index + grid stride stays below 2^32
+    if (V < ((size_t)1 << 31))
+        return tv_launch<T, unsigned>(u, grad, part, part_cap, scal, V, nz, ny, nx, lam, niter,
+                                      height, ylo, yhi, st);
+    return tv_launch<T, size_t>(u, grad, part, part_cap, scal, V, nz, ny, nx, lam, niter, height,
+                                ylo, yhi, st);
 }
 
 // ================================================================ diffusion
