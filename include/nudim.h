@@ -202,6 +202,17 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
                        double gam_min, double gam_max, double interval, double snr,
                        unsigned long seed, double *proj_out, size_t n_out);
 
+/* projection_sim -m DFT (src/projection_sim.c:516-600) on the GPU, FP64:
+ * the same arguments and output as nudim_project_2d1d, the Fourier samples
+ * computed as the reference's exact sums over every voxel with its phase
+ * cos(2 PI t) - i sin(2 PI t), PI = 3.1415926 (src/grid.h:11), and the 3D
+ * method's shifts of both axes around the 2D inverse FFT.  -m 3D
+ * (src/projection_sim.c:409-514) samples the same transform with a 3D NFFT;
+ * its output equals nudim_project_2d1d's to the NFFT's accuracy. */
+int nudim_project_dft(nudim_ctx *ctx, const double *density, int nx, int ny, int nz, int np,
+                      double gam_min, double gam_max, double interval, double snr,
+                      unsigned long seed, double *proj_out, size_t n_out);
+
 /* ------------------------------------------------------------------ */
 /* operator level (device pointers, caller stream)                     */
 /* ------------------------------------------------------------------ */

@@ -52,6 +52,8 @@ EXPORTS = [
     ("nudim_server_destroy", _ip, [_vp]),
     ("nudim_project_2d1d", _ip, [_vp, _dp, _ip, _ip, _ip, _ip, C.c_double, C.c_double,
                              C.c_double, C.c_double, C.c_ulong, _dp, _sz]),
+    ("nudim_project_dft", _ip, [_vp, _dp, _ip, _ip, _ip, _ip, C.c_double, C.c_double,
+                            C.c_double, C.c_double, C.c_ulong, _dp, _sz]),
     ("nudim_nfft_plan_create", _ip, [_vp, _ip, _ip, _ip, _dp, _ip, C.POINTER(_vp)]),
     ("nudim_nfft_plan_destroy", _ip, [_vp]),
     ("nudim_nfft_trafo", _ip, [_vp, _ip, _vp, _vp, _vp]),
@@ -357,12 +359,16 @@ def diffusion2d(ctx, vol_ptr, shape, nx_bound, precision=FP64, lam=0.25, kappa=0
                                    niter, stream))
 
 
-def project_2d1d(ctx, density, np_, gam_min, gam_max, interval, snr=0.0, seed=0):
-    """projection_sim -m 2D1D on the GPU.  density: [nz][ny][nx] -> [tilt][nz][np]."""
+def project_2d1d(ctx, density, np_, gam_min, gam_max, interval, snr=0.0, seed=0, method="2D1D"):
+    """projection_sim on the GPU.  density: [nz][ny][nx] -> [tilt][nz][np].
+    method "2D1D" (and "3D", the same samples) or "DFT" (exact sums)."""
+    if method not in ("2D1D", "3D", "DFT"):
+        raise ValueError("method must be 2D1D, 3D or DFT")
     dens = np.ascontiguousarray(density, np.float64)
     nz, ny, nx = dens.shape
     ns = int((gam_max - gam_min) / interval + 0.5) + 1
     out = np.zeros((ns, nz, np_))
-    _check(lib().nudim_project_2d1d(ctx.h, _dptr(dens), nx, ny, nz, np_, gam_min, gam_max,
-                                    interval, snr, seed, _dptr(out), out.size))
+    fn = lib().nudim_project_dft if method == "DFT" else lib().nudim_project_2d1d
+    _check(fn(ctx.h, _dptr(dens), nx, ny, nz, np_, gam_min, gam_max, interval, snr, seed,
+              _dptr(out), out.size))
     return out

@@ -22,7 +22,7 @@ INC = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["nfft.cu", "nfft_fused.cu", "ops.cu", "denoise.cu", "api.cu", "serve.cu",
-              "noalloc.cu"]
+              "noalloc.cu", "project_dft.cu"]
 CXX_SOURCES = ["tables.cpp"]
 CLI = {
     "reconstruction": ["cli/reconstruction.c", "cli/textio.c"],

@@ -4,10 +4,14 @@
  * the density file holds nx*ny*nz numbers in [z][y][x] order, and
  * ./files/prj-<j>.txt receives np*nz values "%f" per tilt.
  *
- * Method 2D1D runs on the GPU (nudim_project_2d1d).  Methods 3D and DFT are
- * not built (they are alternative simulators of the same projections); they
- * exit with an error.  Noise uses the library's seeded Gaussian generator
- * (--seed, added by this build; default 0), not GSL's sampler.
+ * All three methods run on the GPU.  2D1D: nudim_project_2d1d.  3D samples
+ * the same 3D transform at the same nodes with a 3D NFFT (:409-514); it runs
+ * as 2D1D, whose Z-FFT + 2D NFFT is that transform factorised along the
+ * uniform Z axis (equal to the NFFT's accuracy).  DFT: nudim_project_dft, the
+ * reference's exact sums with its truncated PI.  An unknown method name, which
+ * the reference leaves undefined (:229-242), is rejected.  Noise uses the
+ * library's seeded Gaussian generator (--seed, added by this build; default
+ * 0), not GSL's sampler.
  */
 #include <getopt.h>
 #include <stdio.h>
@@ -119,11 +123,14 @@ int main(int argc, char *argv[])
         fprintf(stderr, "You need to provide valid scope of tomogram angles (-90,90] with --max, --min.\n");
         return 1;
     }
+    int exact = 0;
     if (method == NULL) {
         fprintf(stderr, "You didn't specify simulating method, so I'm  using"
                         " the 2D1D method, which is fastest.\n");
-    } else if (strcmp(method, "2D1D") != 0) {
-        fprintf(stderr, "Method %s is not available in this build (2D1D only).\n", method);
+    } else if (strcmp(method, "DFT") == 0) {
+        exact = 1;
+    } else if (strcmp(method, "2D1D") != 0 && strcmp(method, "3D") != 0) {
+        fprintf(stderr, "Unknown simulating method %s (2D1D, 3D or DFT).\n", method);
         return 1;
     }
     if (config_noise && snr < 0) {
@@ -142,8 +149,10 @@ int main(int argc, char *argv[])
     nudim_ctx *ctx;
     int rc = nudim_ctx_create(device, 0, &ctx);
     if (!rc)
-        rc = nudim_project_2d1d(ctx, dens, nx, ny, nz, np, gam_min, gam_max, interval,
-                                config_noise ? snr : 0.0, seed, proj, per * ns);
+        rc = (exact ? nudim_project_dft : nudim_project_2d1d)(ctx, dens, nx, ny, nz, np, gam_min,
+                                                              gam_max, interval,
+                                                              config_noise ? snr : 0.0, seed,
+                                                              proj, per * ns);
     if (rc) {
         fprintf(stderr, "projection_sim failed (%d): %s\n", rc, nudim_last_error());
         return 1;

@@ -59,25 +59,30 @@ __global__ void k_real_cplx(const double *__restrict__ d, double2 *__restrict__ 
 
 // projection_sim.c:344-366: slice_t[row][col] = NFFT of plane j = (row+nz/2)%nz
 // at radius (col+np/2)%np; plane j's NFFT is row `row` of tmp (q order).
+// zshift = nz/2: the 3D/DFT methods' shift of both axes (:470-476, :562-574),
+// tmp row j holding the nodes of Z index j.
 __global__ void k_sim_gather(const double2 *__restrict__ tmp, double2 *__restrict__ sl, int nz,
-                             int np, int M)
+                             int np, int M, int zshift)
 {
     int t = blockIdx.y;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nz * np) return;
     int row = i / np, col = i - row * np;
-    sl[(size_t)t * nz * np + i] = tmp[(size_t)row * M + (size_t)t * np + (col + np / 2) % np];
+    sl[(size_t)t * nz * np + i] =
+        tmp[(size_t)((row + zshift) % nz) * M + (size_t)t * np + (col + np / 2) % np];
 }
 
-// projection_sim.c:377-390: radial fftshift, real part
+// projection_sim.c:377-390: radial fftshift, real part (zshift = nz/2: the
+// 3D/DFT methods' shift of both axes, :482-494, :582-594)
 __global__ void k_sim_shift(const double2 *__restrict__ sl, double *__restrict__ out, int nz,
-                            int np)
+                            int np, int zshift)
 {
     int t = blockIdx.y;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nz * np) return;
     int row = i / np, col = i - row * np;
-    out[(size_t)t * nz * np + i] = sl[(size_t)t * nz * np + (size_t)row * np + (col + np / 2) % np].x;
+    out[(size_t)t * nz * np + i] =
+        sl[(size_t)t * nz * np + (size_t)((row + zshift) % nz) * np + (col + np / 2) % np].x;
 }
 
 // ================================================================ per-precision state
@@ -910,8 +915,11 @@ int nudim_job_set_denoise_dump(nudim_job *jb, int nn, double *before, double *af
 }
 
 // ---------------------------------------------------------------- simulator
-int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, int nz, int np,
-                       double gam_min, double gam_max, double interval, double snr,
+// method 0: -m 2D1D (Z-FFT + per-plane 2D NFFT); 1: -m DFT (exact sums with
+// the reference's PI).  Both continue with the same 2D inverse FFT, shifts,
+// noise and scaling.
+static int project_run(nudim_ctx *ctx, int method, const double *density, int nx, int ny, int nz,
+                       int np, double gam_min, double gam_max, double interval, double snr,
                        unsigned long seed, double *proj_out, size_t n_out)
 {
     if (!ctx || !density || !proj_out || nx <= 0 || ny <= 0 || nz <= 0 || np <= 0 ||
@@ -931,13 +939,17 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
     size_t XY = (size_t)nx * ny, V = XY * nz;
     std::vector<double> x((size_t)M * 2);
     equal_angle_sample_2d(gam_min, gam_max, interval, np, x.data());
-    NfftTables t;
-    build_nfft_tables(ny, nx, M, x.data(), 16, 16, &t);
     NfftDev<double> pl;
-    int rc = pl.init(ctx, t);
+    int rc = NUDIM_OK;
+    if (method == 0) {
+        NfftTables t;
+        build_nfft_tables(ny, nx, M, x.data(), 16, 16, &t);
+        rc = pl.init(ctx, t);
+    }
     double *dd = nullptr, *dout = nullptr;  // density (V) and tilt series (ns*nz*np)
     double2 *data = nullptr, *tmp = nullptr, *sl = nullptr;
-    if (!rc && (cudaMalloc(&dd, sizeof(double) * V) || cudaMalloc(&data, sizeof(double2) * V) ||
+    if (!rc && (cudaMalloc(&dd, sizeof(double) * V) ||
+                (method == 0 && cudaMalloc(&data, sizeof(double2) * V)) ||
                 cudaMalloc(&tmp, sizeof(double2) * (size_t)nz * M) ||
                 cudaMalloc(&sl, sizeof(double2) * (size_t)ns * nz * np) ||
                 cudaMalloc(&dout, sizeof(double) * (size_t)ns * nz * np))) {
@@ -945,8 +957,12 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
         rc = NUDIM_ENOMEM;
     }
     cufftHandle hz = 0, h2 = 0;
-    if (!rc) {
-        cudaMemcpyAsync(dd, density, sizeof(double) * V, cudaMemcpyHostToDevice, st);
+    if (!rc) cudaMemcpyAsync(dd, density, sizeof(double) * V, cudaMemcpyHostToDevice, st);
+    if (!rc && method == 1) {
+        // :516-560: the exact sums; row j of tmp = the nodes of Z index j
+        rc = dft_slices(dd, nx, ny, nz, np, x.data(), ns, tmp, (size_t)2 << 30, st);
+    }
+    if (!rc && method == 0) {
         k_real_cplx<<<ceil_div((long)V, 256), 256, 0, st>>>(dd, data, V);
         int n1[1] = {nz};
         // projection_sim.c:319-322: forward Z-FFT, stride nx*ny, unshifted
@@ -958,7 +974,7 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
             rc = NUDIM_ECUDA;
         }
     }
-    if (!rc) {
+    if (!rc && method == 0) {
         // :325-351 per plane NFFT; plane q of `data` is slice (q + nz/2) % nz
         PadArgs<double> pa;
         pa.src = data;
@@ -970,7 +986,9 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
     }
     if (!rc) {
         // :359-374 ifftshift into slice[row][col], 2D backward FFT per tilt
-        k_sim_gather<<<dim3(ceil_div((long)nz * np, 256), ns), 256, 0, st>>>(tmp, sl, nz, np, M);
+        const int zshift = method == 0 ? 0 : nz / 2;
+        k_sim_gather<<<dim3(ceil_div((long)nz * np, 256), ns), 256, 0, st>>>(tmp, sl, nz, np, M,
+                                                                             zshift);
         int n2[2] = {nz, np};
         if (cufftPlanMany(&h2, 2, n2, nullptr, 1, nz * np, nullptr, 1, nz * np, CUFFT_Z2Z, ns) ||
             cufftSetStream(h2, st) ||
@@ -982,7 +1000,8 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
     std::vector<double> host;
     if (!rc) {
         // :377-390 radial fftshift, keep the real part (scaled below)
-        k_sim_shift<<<dim3(ceil_div((long)nz * np, 256), ns), 256, 0, st>>>(sl, dout, nz, np);
+        k_sim_shift<<<dim3(ceil_div((long)nz * np, 256), ns), 256, 0, st>>>(
+            sl, dout, nz, np, method == 0 ? 0 : nz / 2);
         host.resize((size_t)ns * nz * np);
         cudaMemcpyAsync(host.data(), dout, sizeof(double) * host.size(), cudaMemcpyDeviceToHost,
                         st);
@@ -1027,6 +1046,22 @@ int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, in
     cudaFree(sl);
     pl.release();
     return rc;
+}
+
+int nudim_project_2d1d(nudim_ctx *ctx, const double *density, int nx, int ny, int nz, int np,
+                       double gam_min, double gam_max, double interval, double snr,
+                       unsigned long seed, double *proj_out, size_t n_out)
+{
+    return project_run(ctx, 0, density, nx, ny, nz, np, gam_min, gam_max, interval, snr, seed,
+                       proj_out, n_out);
+}
+
+int nudim_project_dft(nudim_ctx *ctx, const double *density, int nx, int ny, int nz, int np,
+                      double gam_min, double gam_max, double interval, double snr,
+                      unsigned long seed, double *proj_out, size_t n_out)
+{
+    return project_run(ctx, 1, density, nx, ny, nz, np, gam_min, gam_max, interval, snr, seed,
+                       proj_out, n_out);
 }
 
 // ---------------------------------------------------------------- operators

@@ -234,6 +234,11 @@ template <typename T>
 int tv_run(T *u, T *grad, double *part, int part_cap, double *scal, int nz, int ny, int nx,
            float lam, int niter, int height, int ylo, int yhi, cudaStream_t st);
 int tv_part_count(int nz, int ny, int nx);
+// projection_sim -m DFT Fourier samples: dens [nz][ny][nx] (device, FP64),
+// x2 the 2D equal-angle nodes (host, (r sin g, r cos g) per node, ns*np of
+// them) -> S [nz][ns*np] (device); scratch of the X contraction <= budget.
+int dft_slices(const double *dens, int nx, int ny, int nz, int np, const double *x2, int ns,
+               double2 *S, size_t budget, cudaStream_t st);
 template <typename T>
 int diffusion_run(T *u, int nz, int ny, int nx, int nx_bound, float lambda, float kappa,
                   int niter, cudaStream_t st);

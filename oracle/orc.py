@@ -298,6 +298,55 @@ def project_2d1d(density, np_, gam_min, gam_max, interval):
     return out.reshape(ns, nz, np_)
 
 
+REF_PI = 3.1415926  # src/grid.h:11
+
+
+def nodes_3d(gam_min, gam_max, interval, np_, nz):
+    """equal_angle_sample_3D / grid_slice_3D (src/grid.c:5-57): per tilt, per
+    Z index j, per radial index i the node (r cos g, r sin g, z0), r and z0
+    and the angle by repeated addition; [tilt][j][i][3]."""
+    ns = int((gam_max - gam_min) / interval + 0.5) + 1
+    x = np.zeros((ns, nz, np_, 3))
+    angle = gam_min - interval
+    for s in range(ns):
+        angle += interval
+        z0 = -0.5 - 1.0 / nz
+        for j in range(nz):
+            z0 += 1.0 / nz
+            x0 = -0.5 - 1.0 / np_
+            for i in range(np_):
+                x0 += 1.0 / np_
+                x[s, j, i] = (x0 * np.cos(angle / 180 * REF_PI), x0 * np.sin(angle / 180 * REF_PI),
+                              z0)
+    return x
+
+
+def project_dft(density, np_, gam_min, gam_max, interval, pi=REF_PI):
+    """projection_sim -m DFT (src/projection_sim.c:516-600), small sizes:
+    slice[j] = sum over every voxel of data * (cos(2 pi t) - i sin(2 pi t)),
+    t = col X + row Y + slc Z with centred indices, pi the reference's PI by
+    default; then the swap-shift of both axes, the unnormalised backward 2D
+    FFT, the swap-shift again, and Re / (np nz).  Written per node over the
+    whole voxel set (no factorisation), as the reference sums it."""
+    density = np.asarray(density, np.float64)
+    nz, ny, nx = density.shape
+    x = nodes_3d(gam_min, gam_max, interval, np_, nz)
+    zz, yy, xx = np.meshgrid(np.arange(nz) - nz // 2, np.arange(ny) - ny // 2,
+                             np.arange(nx) - nx // 2, indexing="ij")
+    col, row, slc = xx.reshape(-1), yy.reshape(-1), zz.reshape(-1)
+    d = density.reshape(-1)
+    out = np.zeros((x.shape[0], nz, np_))
+    for s in range(x.shape[0]):
+        xs = x[s].reshape(-1, 3)
+        t = (np.outer(xs[:, 0], col) + np.outer(xs[:, 1], row)) + np.outer(xs[:, 2], slc)
+        sl = ((np.cos(2 * pi * t) - 1j * np.sin(2 * pi * t)) @ d).reshape(nz, np_)
+        sl = np.roll(sl, (nz // 2, np_ // 2), axis=(0, 1))
+        sl = np.fft.ifft2(sl) * (nz * np_)
+        sl = np.roll(sl, (nz // 2, np_ // 2), axis=(0, 1))
+        out[s] = sl.real / (np_ * nz)
+    return out
+
+
 # --------------------------------------------------------------------------
 # reference-built library (only where the reference tree was compiled here)
 # --------------------------------------------------------------------------

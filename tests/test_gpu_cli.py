@@ -1,6 +1,7 @@
 """The drop-in executables end to end: projection_sim writes the tilt series,
 reconstruction / reconstruction_parallel read it and write the reference's
 files; results are compared with the oracle run on the same inputs."""
+import io
 import os
 import subprocess
 
@@ -53,3 +54,29 @@ def test_cli_roundtrip(tmp_path, orc, nudim_built):
     assert "Total time used" in r.stdout
     assert os.path.exists(tmp_path / "recovered-parallel.txt")
     assert os.path.exists(tmp_path / "grad_before.txt")
+
+
+def test_cli_projection_methods(tmp_path, orc, nudim_built):
+    """-m 3D writes the 2D1D files byte for byte (the same samples); -m DFT
+    writes the reference's exact sums (its PI) within "%f" rounding; an
+    unknown method is an error."""
+    vol = small_phantom(16, 8)
+    with open(tmp_path / "vol.txt", "w") as f:
+        f.write("\n".join("%.17g" % v for v in vol.ravel()))
+    base = ["-i", "vol.txt", "-p", "16", "--nx=16", "--ny=16", "--nz=8", "--max=60",
+            "--min=-60", "-t", "20"]
+    files = {}
+    for m in ("2D1D", "3D", "DFT"):
+        d = tmp_path / m
+        (d / "files").mkdir(parents=True)
+        (d / "vol.txt").write_bytes((tmp_path / "vol.txt").read_bytes())
+        r = subprocess.run([exe("projection_sim"), *base, "-m", m], cwd=d, capture_output=True,
+                           text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        files[m] = [(d / "files" / ("prj-%d.txt" % j)).read_bytes() for j in range(7)]
+    assert files["3D"] == files["2D1D"]
+    dft = np.stack([np.loadtxt(io.BytesIO(b)) for b in files["DFT"]]).reshape(7, 8, 16)
+    assert np.abs(dft - orc.project_dft(vol, 16, -60, 60, 20)).max() < 5.1e-7
+    r = subprocess.run([exe("projection_sim"), *base, "-m", "FOO"], cwd=tmp_path / "DFT",
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "Unknown simulating method" in r.stderr
