@@ -384,6 +384,65 @@ def serving_bench(ctx, n_jobs, rate, precision, seed=20261205):
     return st
 
 
+def large_bench(ctx, steps=10, warmup=3):
+    """The large-volume configuration: 512 x 512 x 256 blob + shell phantom,
+    121 tilts (-60..60 step 1) at SNR 0.3, reconstructed at np = nx = 768,
+    nz = 256 with --weight and TV; the mixed form with an FP64 corrective
+    iteration every 10 iterations.  Timed: `steps` iterations after `warmup`
+    (with steps = 10, exactly one corrective iteration), CUDA events on the
+    job's stream.  Accuracy: relative L2 against the FP64 plain form after
+    1 and after warmup + steps iterations, with and without the correction."""
+    import nudim_gb300 as ng
+    from nudim_gb300.synth import CONFIGS, MASTER_SEED, make_inputs
+    c = CONFIGS["cfg5"]
+    r = dict(c["recon"])
+    t0 = time.perf_counter()
+    vol, proj = make_inputs(ctx, "cfg5", seed=MASTER_SEED)
+    del vol
+    t_inputs = time.perf_counter() - t0
+    total = warmup + steps
+    V = r["nz"] * r["np"] ** 2
+    snaps = {}
+
+    def run(precision, correct, timed):
+        kw = job_kwargs(r, precision)
+        kw["correct_every"] = correct
+        t0 = time.perf_counter()
+        job = ng.Job(ctx, **kw)
+        job.set_projections(proj)
+        t_setup = time.perf_counter() - t0
+        job.step(1)
+        v1 = job.volume()
+        job.step(warmup - 1)
+        ms = timed_steps(ctx, job, steps) if timed else None
+        if not timed:
+            job.step(steps)
+        vN = job.volume()
+        job.close()
+        return v1, vN, ms, t_setup
+
+    v1c, vNc, ms, t_setup = run(ng.MIXED, 10, True)
+    log("large: %.1f ms/iteration (mixed, FP64 correction every 10)" % (ms / steps))
+    v1m, vNm, ms_plain, _ = run(ng.MIXED, 0, True)
+    v164, vN64, ms64, _ = run(ng.FP64, 0, True)
+    rl = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    out = {"value": V * steps / (ms / 1e3), "unit": "voxel-iters/s", "steps": steps,
+           "warmup": warmup, "ms_per_step": ms / steps,
+           "mixed_plain_ms_per_step": ms_plain / steps, "fp64_ms_per_step": ms64 / steps,
+           "config": {"workload": "512x512x256 blob+shell phantom, 121 tilts -60..60 step 1, "
+                                  "SNR 0.3, np=nx=768, nz=256, padangle 1, --weight, TV, "
+                                  "FP64 correction every 10 iterations",
+                      "voxels": V},
+           "rel_l2_vs_fp64_after_1": {"corrected": rl(v1c, v164), "mixed": rl(v1m, v164)},
+           "rel_l2_vs_fp64_after_%d" % total: {"corrected": rl(vNc, vN64),
+                                               "mixed": rl(vNm, vN64)},
+           "setup_s": t_setup, "inputs_s": t_inputs}
+    log("large: %.3e voxel-iters/s, vs FP64 after %d: corrected %.2e, mixed %.2e"
+        % (out["value"], total, out["rel_l2_vs_fp64_after_%d" % total]["corrected"],
+           out["rel_l2_vs_fp64_after_%d" % total]["mixed"]))
+    return out
+
+
 # ------------------------------------------------------------------ arms
 def run_reference(args):
     ws, rank, local = dist_env()
@@ -552,6 +611,8 @@ def run_ours(args):
         line["mixed_over_fp64"] = value / v64
         line["rel_l2_mixed_vs_fp64_after_1_iteration"] = err1
         line["rel_l2_mixed_vs_fp64_after_warmup"] = err
+    if args.large:
+        line["large"] = large_bench(ctx)
     if args.batch_jobs > 0:
         line["batched"] = {"mixed": batched_bench(ctx, args.batch_jobs, args.steps, args.warmup,
                                                   ng.MIXED)}
@@ -581,6 +642,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--large", action="store_true",
+                    help="also run the large-volume configuration (768^2 x 256, ~3 min)")
     ap.add_argument("--batch-jobs", type=int, default=48,
                     help="jobs in the batched measurement (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=16,
