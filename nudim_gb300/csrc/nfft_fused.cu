@@ -291,15 +291,18 @@ k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int 
         for (int q = 0; q < cnt; q++) {
             const C *gp = G + (size_t)((cl0 + q) & (BC - 1)) * n0;
             T sr = 0, si = 0;
-            if (sizeof(T) == 4) {
+            if constexpr (sizeof(T) == 4) {
+                // FP32 form: one paired FMA per row, (re, im) += q * g
+                float2 s2 = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int i = 0; i < 8; i++) {
                     float4 pr = *(const float4 *)(gp + ((rb + 2 * i) & m0));
-                    sr += qa[2 * i] * (T)pr.x;
-                    si += qa[2 * i] * (T)pr.y;
-                    sr += qa[2 * i + 1] * (T)pr.z;
-                    si += qa[2 * i + 1] * (T)pr.w;
+                    s2 = __ffma2_rn(make_float2(qa[2 * i], qa[2 * i]), make_float2(pr.x, pr.y), s2);
+                    s2 = __ffma2_rn(make_float2(qa[2 * i + 1], qa[2 * i + 1]),
+                                    make_float2(pr.z, pr.w), s2);
                 }
+                sr = s2.x;
+                si = s2.y;
             } else {
 #pragma unroll
                 for (int i = 0; i < 16; i++) {
@@ -436,7 +439,7 @@ k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     const int R = 32 / BC, W = R + BC;
     unsigned char *wst = (unsigned char *)(K + buf) + warp * spread_stage_bytes<T, P>(W);
-    C *fs = (C *)wst;                        // [P][NB]
+    C *fs = (C *)wst;                        // [NB][P]
     T *ws = (T *)(fs + P * NB);              // [2][NB * W]
     int *jb = (int *)(ws + 2 * NB * W);      // [2][NB]
     const int rr = lane / BC, cc = lane - rr * BC;
@@ -514,32 +517,42 @@ k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
                     fv = sa.f[(size_t)(plane0 + pb + p) * sa.f_stride + jl];
                     if (WEIGHTED) fv = mkc<T>(wv * fv.x, wv * fv.y);
                 }
-                fs[p * NB + lane] = fv;
+                fs[lane * P + p] = fv;
             }
         }
         __syncwarp();
         const T *wc = ws + sb * NB * W;
-        T br[P], bi[P];
+        float2 bs[P];  // FP32 form: the batch sums (re, im) of each plane
 #pragma unroll
-        for (int p = 0; p < P; p++) br[p] = bi[p] = T(0);
+        for (int p = 0; p < P; p++) bs[p] = make_float2(0.f, 0.f);
         // nodes k0 .. k0 + K of the batch (weights past the list end are zero)
         auto nodes = [&](auto kcount) {
             constexpr int K = decltype(kcount)::value;
 #pragma unroll
             for (int k = 0; k < K; k++) {
                 T q0 = wc[k * W + rr], q1 = wc[k * W + R + cc];
-                if (sizeof(T) == 4) {
-                    T q = q0 * q1;
+                if constexpr (sizeof(T) == 4) {
+                    // one paired FMA per plane: (re, im) += q * f
+                    const float q = q0 * q1;
+                    const float2 qq = make_float2(q, q);
+                    if constexpr (P % 2 == 0) {
 #pragma unroll
-                    for (int p = 0; p < P; p++) {
-                        C fv = fs[p * NB + k];
-                        br[p] += q * fv.x;
-                        bi[p] += q * fv.y;
+                        for (int p = 0; p < P; p += 2) {
+                            const float4 f2 = *reinterpret_cast<const float4 *>(fs + k * P + p);
+                            bs[p] = __ffma2_rn(qq, make_float2(f2.x, f2.y), bs[p]);
+                            bs[p + 1] = __ffma2_rn(qq, make_float2(f2.z, f2.w), bs[p + 1]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int p = 0; p < P; p++) {
+                            const C fv = fs[k * P + p];
+                            bs[p] = __ffma2_rn(qq, make_float2(fv.x, fv.y), bs[p]);
+                        }
                     }
                 } else {
 #pragma unroll
                     for (int p = 0; p < P; p++) {
-                        C fv = fs[p * NB + k];
+                        C fv = fs[k * P + p];
                         ar[p] += q1 * (q0 * fv.x);
                         ai[p] += q1 * (q0 * fv.y);
                     }
@@ -549,11 +562,11 @@ k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
         // a short batch (the tail of most lists) runs the half-length loop
         if (n <= NB / 2) nodes(std::integral_constant<int, NB / 2>());
         else nodes(std::integral_constant<int, NB>());
-        if (sizeof(T) == 4) {
+        if constexpr (sizeof(T) == 4) {
 #pragma unroll
             for (int p = 0; p < P; p++) {
-                kr[p].add(br[p]);
-                ki[p].add(bi[p]);
+                kr[p].add(bs[p].x);
+                ki[p].add(bs[p].y);
             }
         }
         __syncwarp();  // stage sb and fs are refilled two steps on
