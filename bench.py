@@ -632,6 +632,43 @@ def run_ours(args):
     return 0
 
 
+def tv_micro(args):
+    """nudim_tv alone: a seeded N(0, 0.3^2) volume of the given shape, 40 inner
+    iterations per call, `warmup` untimed calls then `steps` calls timed with
+    CUDA events on the launching stream; FP32 form, then FP64 (one call)."""
+    import torch
+
+    import nudim_gb300 as ng
+    from nudim_gb300 import build as nb
+    nb.build()
+    shape = tuple(int(v) for v in args.tv.lower().split("x"))
+    ctx = ng.Context(0)
+    out = {"metric": "TV inner iterations x voxels per second", "shape": list(shape)}
+    V = int(np.prod(shape))
+    for prec, name, steps in ((ng.MIXED, "fp32", args.steps), (ng.FP64, "fp64", 1)):
+        dt = torch.float32 if prec == ng.MIXED else torch.float64
+        g = torch.Generator().manual_seed(1)
+        v = (torch.randn(shape, dtype=torch.float64, generator=g) * 0.3).to(dt).cuda()
+        st = torch.cuda.current_stream()
+        for _ in range(args.warmup if prec == ng.MIXED else 1):
+            ng.tv(ctx, v.data_ptr(), shape, prec, 0.2, 40, stream=st.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            ng.tv(ctx, v.data_ptr(), shape, prec, 0.2, 40, stream=st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[name] = {"ms_per_call": ms, "ms_per_inner_iteration": ms / 40,
+                     "value": 40 * V / (ms / 1e3),
+                     "bytes_per_inner_iteration": 5 * (4 if prec == ng.MIXED else 8) * V}
+        log("tv %s %s: %.2f ms per 40 inner iterations" % (name, args.tv, ms))
+    ctx.close()
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -652,11 +689,16 @@ def main():
     ap.add_argument("--serve-fp64", action="store_true", help="also serve the FP64 form")
     ap.add_argument("--nz", type=int, default=0,
                     help="override the number of Z-planes (small-case profiling only)")
+    ap.add_argument("--tv", default="",
+                    help="NZxNYxNX: only time nudim_tv (40 inner iterations) on a volume of "
+                         "that shape in both forms (a kernel micro-benchmark)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     global NZ_OVERRIDE
     NZ_OVERRIDE = args.nz or None
+    if args.tv:
+        return tv_micro(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -16,7 +16,7 @@ namespace nudim {
 // One TV iteration is two launches:
 //   k_tv_grad   the gradient g of every voxel and the two global sums
 //               (sum g^2, sum of squares of the negative voxels).  A block
-//               owns a 32 x 8 (x, y) tile and a run of Z-planes; it marches
+//               owns a 32 x 16 (x, y) tile and a run of Z-planes; it marches
 //               along Z with three planes of the tile plus a one-cell halo in
 //               shared memory, so every voxel is read from memory about once.
 //               The halo cells hold the clamped neighbours (index -1 -> 0,
@@ -24,7 +24,8 @@ namespace nudim {
 //               The block that finishes last sums the per-block partials in
 //               block order (deterministic) into scal[0..1];
 //   k_tv_update u -= (lam sqrt(scal[1])) (g / sqrt(scal[0])).
-constexpr int kTvTX = 32, kTvTY = 8, kTvSX = kTvTX + 2, kTvSY = kTvTY + 2;
+constexpr int kTvTX = 32, kTvTY = 16, kTvSX = kTvTX + 2, kTvSY = kTvTY + 2;
+constexpr int kTvRows = kTvTY / 8;  // rows per thread (256 threads = 8 warps of 32 x)
 
 // Gradient of voxel (i, j, k) (denoise.c:84-122) from three tile planes:
 // p = plane clamp(i-1), q = plane i, r = plane clamp(i+1), the voxel at
@@ -73,6 +74,39 @@ __device__ __forceinline__ T tv_point(const T (*p)[kTvSX], const T (*q)[kTvSX],
     return rn_sub(rn_sub(rn_sub(g1, g2), g3), g4);
 }
 
+// FP32 form, two voxels at once: tile cells (y, x) and (y + 8, x), each
+// operation of tv_point paired (one paired add / fused multiply-add / multiply
+// for both voxels); c returns both centre values.
+__device__ __forceinline__ float2 tv_point2(const float (*p)[kTvSX], const float (*q)[kTvSX],
+                                            const float (*r)[kTvSX], int y, int x, float2 &c)
+{
+    auto ld = [&](const float (*a)[kTvSX], int yy, int xx) {
+        return make_float2(a[yy][xx], a[yy + 8][xx]);
+    };
+    auto sub = [](float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); };
+    c = ld(q, y, x);
+    const float2 t1 = sub(c, ld(p, y, x)), t2 = sub(c, ld(q, y - 1, x)),
+                 t3 = sub(c, ld(q, y, x - 1));
+    const float2 a4 = ld(r, y, x);
+    const float2 t4 = sub(a4, c), t5 = sub(a4, ld(r, y - 1, x)), t6 = sub(a4, ld(r, y, x - 1));
+    const float2 a7 = ld(q, y + 1, x);
+    const float2 t7 = sub(a7, ld(p, y + 1, x)), t8 = sub(a7, c),
+                 t9 = sub(a7, ld(q, y + 1, x - 1));
+    const float2 a10 = ld(q, y, x + 1);
+    const float2 t10 = sub(a10, ld(p, y, x + 1)), t11 = sub(a10, ld(q, y - 1, x + 1)),
+                 t12 = sub(a10, c);
+    const float2 e2 = make_float2(1e-8f, 1e-8f);
+    auto inv = [&](float2 a, float2 b, float2 d) {
+        float2 s = __ffma2_rn(d, d, __ffma2_rn(b, b, __ffma2_rn(a, a, e2)));
+        return make_float2(rsqrtf(s.x), rsqrtf(s.y));
+    };
+    const float2 h1 = __fmul2_rn(__fadd2_rn(__fadd2_rn(t1, t2), t3), inv(t1, t2, t3));
+    const float2 h2 = __fmul2_rn(t4, inv(t4, t5, t6));
+    const float2 h3 = __fmul2_rn(t8, inv(t7, t8, t9));
+    const float2 h4 = __fmul2_rn(t12, inv(t10, t11, t12));
+    return sub(sub(sub(h1, h2), h3), h4);
+}
+
 // A thread's running sum of its voxels' terms: plain in the FP64 form,
 // Neumaier-compensated in the FP32 form (a thread sums one term per plane of
 // its Z-run).
@@ -94,8 +128,8 @@ template <typename T> struct TvAcc {
 // The two sums: FP64 products and sums in the FP64 form; FP32 products and
 // compensated per-thread sums, FP32 warp sums and FP64 across warps and
 // blocks in the FP32 form.  Grid (x tiles, y tiles, Z-runs of zc planes);
-// 256 threads, thread (ty, tx) owns column (j0 + ty, k0 + tx).  done: a
-// zeroed counter (the last block resets it).
+// 256 threads, thread (ty, tx) owns the columns (j0 + ty + 8 r, k0 + tx),
+// r < kTvRows.  done: a zeroed counter (the last block resets it).
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part,
@@ -109,8 +143,13 @@ k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part,
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int k0 = blockIdx.x * kTvTX, j0 = blockIdx.y * kTvTY;
     const int z0 = blockIdx.z * zc, z1 = min(nz, z0 + zc);
-    const int k = k0 + tx, j = j0 + ty;
-    const bool own = k < nx && j < ny && (!height || (j >= ylo && j <= yhi));
+    const int k = k0 + tx;
+    bool own[kTvRows];
+#pragma unroll
+    for (int r = 0; r < kTvRows; r++) {
+        const int j = j0 + ty + 8 * r;
+        own[r] = k < nx && j < ny && (!height || (j >= ylo && j <= yhi));
+    }
     const size_t P = (size_t)ny * nx;
     // this thread's halo-tile cells and their clamped in-plane offsets
     int cell[kSlots];
@@ -145,12 +184,27 @@ k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part,
     TvAcc<T> ag, an;
     for (int i = z0; i < z1; i++) {
         if (i + 1 < z1) fetch(min(i + 2, nz - 1));  // in flight during the compute
-        if (own) {
-            T c;
-            T gv = tv_point<T>(pl[bp], pl[bc], pl[bn], ty + 1, tx + 1, c);
-            g[(size_t)i * P + (size_t)j * nx + k] = gv;
-            ag.add(rn_mul(gv, gv));
-            if (c < T(0)) an.add(rn_mul(c, c));
+        if constexpr (sizeof(T) == 4 && kTvRows == 2) {
+            float2 c2;
+            const float2 g2 = tv_point2(pl[bp], pl[bc], pl[bn], ty + 1, tx + 1, c2);
+            const float gv[2] = {g2.x, g2.y}, cv[2] = {c2.x, c2.y};
+#pragma unroll
+            for (int r = 0; r < 2; r++)
+                if (own[r]) {
+                    g[(size_t)i * P + (size_t)(j0 + ty + 8 * r) * nx + k] = gv[r];
+                    ag.add(rn_mul(gv[r], gv[r]));
+                    if (cv[r] < 0.f) an.add(rn_mul(cv[r], cv[r]));
+                }
+        } else {
+#pragma unroll
+            for (int r = 0; r < kTvRows; r++)
+                if (own[r]) {
+                    T c;
+                    T gv = tv_point<T>(pl[bp], pl[bc], pl[bn], ty + 8 * r + 1, tx + 1, c);
+                    g[(size_t)i * P + (size_t)(j0 + ty + 8 * r) * nx + k] = gv;
+                    ag.add(rn_mul(gv, gv));
+                    if (c < T(0)) an.add(rn_mul(c, c));
+                }
         }
         __syncthreads();
         if (i + 1 < z1) {
