@@ -434,7 +434,7 @@ k_diffusion(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, int ni
 // position y - y0(d)).  During step t diagonal t + 2 is fetched into
 // registers (its slot held diagonal t + 2 - R, written back at step t - 1)
 // and diagonal t - 2G + 1, final for the group, is written back: one barrier
-// per step.  The cells of a step are dealt out as 64-cell segments of the
+// per step.  The cells of a step are dealt out as 128-cell segments of the
 // active diagonals, one warp per segment, from a task table (segment prefix
 // counts and ring slots) that warp 0 builds for step t + 1 during step t.
 // Requires min(ny, nx) <= kDiffPf * blockDim.x.
@@ -453,9 +453,9 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
     const int D = ny + nx - 1, L = min(ny, nx);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     // per step (double-buffered), for active diagonal k (sweep g_lo + k):
-    // prefix count of its 64-cell tasks, d, y0(d), len(d), and the ring offsets
+    // prefix count of its 128-cell tasks, d, y0(d), len(d), and the ring offsets
     // of diagonals d, d - 1, d + 1
-    constexpr int TC = 64;
+    constexpr int TC = 128;
     __shared__ int s_pre[2][kDiffMaxG + 1], s_meta[2][2];
     __shared__ int4 s_dg[2][kDiffMaxG];   // d, y0, len, ring offset of d
     __shared__ int2 s_nb[2][kDiffMaxG];   // ring offsets of d - 1 (d itself when d == 0) and d + 1
@@ -509,14 +509,17 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
             // fetch diagonal t + 2
             const int dn = t + 2;
             const int nn = dn < D ? len(dn) : 0;
+            // slots a diagonal of this plane can use (uniform: a real branch)
+            const int npf = (L + blockDim.x - 1) / blockDim.x;
             T pf[kDiffPf];
 #pragma unroll
             for (int k = 0; k < kDiffPf; k++) {
+                if (k >= npf) break;
                 int i = threadIdx.x + k * blockDim.x;
                 pf[k] = i < nn ? U[cell(dn, i)] : T(0);
             }
             // the next step's task table (warp 0), then this step's tasks:
-            // 64-cell segments of the active diagonals, dealt out to the warps
+            // 128-cell segments of the active diagonals, dealt out to the warps
             const int tb = t & 1;
             if (warp == 0 && t + 1 < nsteps) build_table(t + 1, gc, tb ^ 1);
             {
@@ -580,6 +583,7 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
                 T *s = slot(dn);
 #pragma unroll
                 for (int k = 0; k < kDiffPf; k++) {
+                    if (k >= npf) break;
                     int i = threadIdx.x + k * blockDim.x;
                     if (i < nn) s[i] = pf[k];
                 }
