@@ -212,24 +212,36 @@ k_rowfft(const void *__restrict__ src, size_t src_stride, int N0, int N1, int n1
     C *A = (C *)smraw, *B = A + fft_buf((size_t)kRows * n1);
     int b = blockIdx.y, gb = plane0 + b, a0 = blockIdx.x * kRows;
     int nr = min(kRows, N0 - a0);
-    for (int idx = threadIdx.x; idx < nr * n1; idx += blockDim.x) {
-        int r = idx / n1, l1 = idx - r * n1;
-        int k1 = l1 < n1 / 2 ? l1 : l1 - n1;
-        C v = mkc<T>(0, 0);
-        if (k1 >= -N1 / 2 && k1 < N1 / 2) {
-            int a = a0 + r, c = k1 + N1 / 2;
-            size_t o = (size_t)gb * src_stride + (size_t)a * N1 + c;
-            C s;
-            if (MODE == PM_COMPLEX) {
-                s = ((const C *)src)[o];
-            } else {
-                s = mkc<T>(((const T *)src)[o], T(0));
-                f_init[(size_t)gb * f_stride + (size_t)a * N1 + c] = s;
+    // eight elements per thread in flight before the shared-memory stores
+    constexpr int U = 8;
+    const int total = nr * n1;
+    for (int base = threadIdx.x; base < total; base += U * blockDim.x) {
+        C v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int idx = base + u * blockDim.x;
+            const int r = idx / n1, l1 = idx - r * n1;
+            const int k1 = l1 < n1 / 2 ? l1 : l1 - n1;
+            v[u] = mkc<T>(0, 0);
+            if (idx < total && k1 >= -N1 / 2 && k1 < N1 / 2) {
+                int a = a0 + r, c = k1 + N1 / 2;
+                size_t o = (size_t)gb * src_stride + (size_t)a * N1 + c;
+                C s;
+                if (MODE == PM_COMPLEX) {
+                    s = ((const C *)src)[o];
+                } else {
+                    s = mkc<T>(((const T *)src)[o], T(0));
+                    f_init[(size_t)gb * f_stride + (size_t)a * N1 + c] = s;
+                }
+                T sc = c0[a] * c1[c];
+                v[u] = mkc<T>(s.x * sc, s.y * sc);
             }
-            T sc = c0[a] * c1[c];
-            v = mkc<T>(s.x * sc, s.y * sc);
         }
-        A[idx] = v;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int idx = base + u * blockDim.x;
+            if (idx < total) A[idx] = v[u];
+        }
     }
     __syncthreads();
     C *R = block_fft<T, -1>(A, B, n1, logn1, nr, tw1);
@@ -268,14 +280,29 @@ k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int 
     C *A = (C *)smraw, *B = A + fft_buf((size_t)BC * n0);
     int cb = blockIdx.x, b = blockIdx.y;
     const C *Hb = H + (size_t)b * N0 * n1 + (size_t)cb * BC;
-    // rows a of H land at l0 = (a - N0/2) mod n0; the other rows are zero
-#pragma unroll 4
-    for (int idx = threadIdx.x; idx < n0 * BC; idx += blockDim.x) {
-        int l0 = idx / BC, c = idx - l0 * BC;
-        int k0 = l0 < n0 / 2 ? l0 : l0 - n0;
-        C v = mkc<T>(0, 0);
-        if (k0 >= -N0 / 2 && k0 < N0 / 2) v = Hb[(size_t)(k0 + N0 / 2) * n1 + c];
-        A[(size_t)c * n0 + l0] = v;
+    // rows a of H land at l0 = (a - N0/2) mod n0; the other rows are zero.
+    // Eight loads per thread in flight before the shared-memory stores.
+    {
+        constexpr int U = 8;
+        const int total = n0 * BC;
+        for (int base = threadIdx.x; base < total; base += U * blockDim.x) {
+            C v[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int idx = base + u * blockDim.x;
+                const int l0 = idx / BC, c = idx - l0 * BC;
+                const int k0 = l0 < n0 / 2 ? l0 : l0 - n0;
+                v[u] = mkc<T>(0, 0);
+                if (idx < total && k0 >= -N0 / 2 && k0 < N0 / 2)
+                    v[u] = Hb[(size_t)(k0 + N0 / 2) * n1 + c];
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int idx = base + u * blockDim.x;
+                const int l0 = idx / BC, c = idx - l0 * BC;
+                if (idx < total) A[(size_t)c * n0 + l0] = v[u];
+            }
+        }
     }
     __syncthreads();
     const C *G = block_fft<T, -1>(A, B, n0, logn0, BC, tw0);
@@ -619,7 +646,28 @@ k_rowifft_crop(const cplx_t<T> *__restrict__ Hp, int N0, int N1, int n1, int log
     int b = blockIdx.y, gb = plane0 + b, a0 = blockIdx.x * kRows;
     int nr = min(kRows, N0 - a0);
     const C *Hb = Hp + ((size_t)b * N0 + a0) * n1;
-    for (int idx = threadIdx.x; idx < nr * n1; idx += blockDim.x) A[idx] = Hb[idx];
+    {
+        // the nr contiguous rows as 16-byte vectors, eight per thread in
+        // flight before the shared-memory stores
+        using V = float4;
+        const int nv = nr * n1 * (int)sizeof(C) / 16;
+        const V *src = reinterpret_cast<const V *>(Hb);
+        V *dst = reinterpret_cast<V *>(A);
+        constexpr int U = 8;
+        for (int base = threadIdx.x; base < nv; base += U * blockDim.x) {
+            V v[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int i = base + u * blockDim.x;
+                if (i < nv) v[u] = src[i];
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int i = base + u * blockDim.x;
+                if (i < nv) dst[i] = v[u];
+            }
+        }
+    }
     __syncthreads();
     C *R = block_fft<T, +1>(A, B, n1, logn1, nr, tw1);
     T s = 0;
