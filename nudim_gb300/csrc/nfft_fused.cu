@@ -358,13 +358,21 @@ k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ 
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     T s0 = 0, s1 = 0;
     if (j < M) {
-        int ns = nslots[j];
-        C f = part[((size_t)b * smax) * M + j];
-        for (int s = 1; s < ns; s++) {
-            C v = part[((size_t)b * smax + s) * M + j];
-            f.x += v.x;
-            f.y += v.y;
-        }
+        // the node's partials (at most 8 slots) loaded together, summed in
+        // slot order
+        const int ns = nslots[j];
+        C v[8];
+        v[0] = part[((size_t)b * smax) * M + j];
+#pragma unroll
+        for (int s = 1; s < 8; s++)
+            if (s < ns) v[s] = part[((size_t)b * smax + s) * M + j];
+        C f = v[0];
+#pragma unroll
+        for (int s = 1; s < 8; s++)
+            if (s < ns) {
+                f.x += v[s].x;
+                f.y += v[s].y;
+            }
         size_t o = (size_t)gb * a.out_stride + j;
         if (MODE == IM_PLAIN) {
             a.out[o] = f;
