@@ -29,7 +29,8 @@ constexpr int kTvRows = kTvTY / 8;  // rows per thread (256 threads = 8 warps of
 
 // Gradient of voxel (i, j, k) (denoise.c:84-122) from three tile planes:
 // p = plane clamp(i-1), q = plane i, r = plane clamp(i+1), the voxel at
-// tile cell (y, x).
+// tile cell (y, x); the reference's IEEE operations in its order (the FP64
+// form; the FP32 form runs tv_point2).
 template <typename T>
 __device__ __forceinline__ T tv_point(const T (*p)[kTvSX], const T (*q)[kTvSX],
                                       const T (*r)[kTvSX], int y, int x, T &c)
@@ -51,19 +52,6 @@ __device__ __forceinline__ T tv_point(const T (*p)[kTvSX], const T (*q)[kTvSX],
     T t10 = rn_sub(a10, p[y][x + 1]);
     T t11 = rn_sub(a10, q[y - 1][x + 1]);
     T t12 = rn_sub(a10, c);
-    if (sizeof(T) == 4) {
-        // FP32 form: t / sqrt(eps + x^2 + y^2 + z^2) as t * rsqrt(...) with
-        // fused multiply-adds (a few ulp per term, against one for IEEE sqrt
-        // and division; the loop's own amplification of rounding dominates)
-        auto inv = [&](float x, float y, float z) {
-            return rsqrtf(fmaf(z, z, fmaf(y, y, fmaf(x, x, (float)eps))));
-        };
-        float h1 = ((float)t1 + (float)t2 + (float)t3) * inv(t1, t2, t3);
-        float h2 = (float)t4 * inv(t4, t5, t6);
-        float h3 = (float)t8 * inv(t7, t8, t9);
-        float h4 = (float)t12 * inv(t10, t11, t12);
-        return (T)(h1 - h2 - h3 - h4);
-    }
     auto nrm = [&](T x, T y, T z) {
         return rn_sqrt(rn_add(rn_add(rn_add(eps, rn_mul(x, x)), rn_mul(y, y)), rn_mul(z, z)));
     };
@@ -75,8 +63,11 @@ __device__ __forceinline__ T tv_point(const T (*p)[kTvSX], const T (*q)[kTvSX],
 }
 
 // FP32 form, two voxels at once: tile cells (y, x) and (y + 8, x), each
-// operation of tv_point paired (one paired add / fused multiply-add / multiply
-// for both voxels); c returns both centre values.
+// operation paired (one paired add / fused multiply-add / multiply for both
+// voxels); t / sqrt(eps + x^2 + y^2 + z^2) as t * rsqrt(...) with fused
+// multiply-adds (a few ulp per term, against one for IEEE sqrt and division;
+// the TV loop's own amplification of rounding dominates).  c returns both
+// centre values.
 __device__ __forceinline__ float2 tv_point2(const float (*p)[kTvSX], const float (*q)[kTvSX],
                                             const float (*r)[kTvSX], int y, int x, float2 &c)
 {
