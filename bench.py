@@ -563,16 +563,24 @@ def run_ours(args):
         barrier(dist)
         t0 = time.perf_counter()
         job = ng.Job(ctx, **job_kwargs(r, ng.MIXED))
+        t1 = time.perf_counter()
         job.set_projections(proj)
+        job.sync()
+        t2 = time.perf_counter()
         job.step(args.steps)
+        job.sync()
+        t3 = time.perf_counter()
         out = job.volume()
         t_e2e = time.perf_counter() - t0
+        phases = {"job_create_s": t1 - t0, "set_projections_s": t2 - t1,
+                  "iterations_s": t3 - t2, "volume_to_host_s": t0 + t_e2e - t3}
         job.close()
         t_e2e = max_over_ranks(dist, t_e2e, dev)
         e2e = {"value": ws * V * args.steps / t_e2e, "unit": "voxel-iters/s",
                "h2d_bytes_per_step": int(proj.nbytes // args.steps),
                "d2h_bytes_per_step": int(out.nbytes // args.steps),
-               "includes": "job setup (tilt-series NFFT, slice reorder, initial inverse NFFT)"}
+               "includes": "job setup (tilt-series NFFT, slice reorder, initial inverse NFFT)",
+               "phases": phases}
         log("e2e: %.3e voxel-iters/s" % e2e["value"])
 
     # ---- FP64 plain form on the same job (fewer steps: it is the slow form)

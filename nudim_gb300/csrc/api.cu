@@ -152,7 +152,9 @@ struct nudim_job {
     JobState<float> s32;
     int dump_nn = -1;
     double *dump_before = nullptr, *dump_after = nullptr;
-    std::vector<double> vol0;
+    // the initial volume (reconstruction.c:521-540, recovered-0.txt) kept on
+    // the device in the job's precision; sent to the host only on request
+    void *vol0 = nullptr;
 };
 
 struct nudim_nfft_plan {
@@ -259,8 +261,11 @@ static int iters_of(const nudim_job *jb) { return jb->d.cgnr_iters > 0 ? jb->d.c
 
 // Slices, initial inverse NFFT and backward Z-FFT for state s.
 template <typename T>
+// inverse = false: only the measured samples (the FP64 state of a mixed job
+// with correction, whose volume is taken from the FP32 state before each
+// corrective iteration)
 static int state_setup(nudim_job *jb, JobState<T> &s, const double2 *tomo, const int *d_order,
-                       const int *d_rank, const double *d_fill)
+                       const int *d_rank, const double *d_fill, bool inverse = true)
 {
     cudaStream_t st = jb->stream;
     int nz = jb->d.nz, np = jb->d.np, M = jb->M;
@@ -268,6 +273,7 @@ static int state_setup(nudim_job *jb, JobState<T> &s, const double2 *tomo, const
     k_build_slices<T><<<dim3(ceil_div(M, 256), nz), 256, 0, st>>>(
         tomo, s.known, d_order, d_rank, d_fill, jb->n_unk_row, np, nz, M, s.slices);
     NUDIM_LAUNCH_CHECK();
+    if (!inverse) return NUDIM_OK;
     // reconstruction.c:495-518: f = 0, before_loop + 10 steps, per plane
     CgnrBuffers<T> b = cg_bufs(s);
     NUDIM_TRY(cgnr_run<T>(s.pl, nz, s.slices, s.w, s.data, nullptr, true, iters_of(jb), b, st));
@@ -477,7 +483,7 @@ static size_t job_bytes(const nudim_job_desc *d, int A, bool both, size_t fused_
     size_t n1 = (size_t)grid_size(d->np);
     auto per = [&](size_t sT) {
         size_t sC = 2 * sT;
-        size_t b = 2 * V * sT + 3 * V * sC + 4 * nz * M * sC;
+        size_t b = 3 * V * sT + 3 * V * sC + 4 * nz * M * sC;  // + the initial volume
         if (d->denoise == NUDIM_DENOISE_TV) b += V * sT;
         b += M * (8 + 28 * sT + 20);  // node tables and tile lists
         // fused-path lists: ~11 adjoint tile entries and <= 5 trafo entries per
@@ -681,6 +687,7 @@ int nudim_job_destroy(nudim_job *jb)
     jb->s64.release();
     jb->s32.release();
     ws_release(&jb->ws);
+    if (jb->vol0) cudaFreeAsync(jb->vol0, jb->stream);
     cudaStreamSynchronize(jb->stream);
     cudaStreamDestroy(jb->stream);
     delete jb;
@@ -788,13 +795,25 @@ int nudim_job_set_projections(nudim_job *jb, const double *proj, size_t n)
         else {
             rc = state_setup<float>(jb, jb->s32, d_tomo, d_order, d_rank, d_fill);
             if (!rc && jb->s64.live)
-                rc = state_setup<double>(jb, jb->s64, d_tomo, d_order, d_rank, d_fill);
+                rc = state_setup<double>(jb, jb->s64, d_tomo, d_order, d_rank, d_fill, false);
         }
     }
     if (!rc) {
+        // keep the initial volume: a device copy of the state's volume
         size_t V = (size_t)d.np * d.np * d.nz;
-        jb->vol0.resize(V);
-        rc = nudim_job_get_volume(jb, jb->vol0.data(), V, 0);
+        size_t bytes = V * (d.precision == NUDIM_FP64 ? sizeof(double) : sizeof(float));
+        const void *src = d.precision == NUDIM_FP64 ? (const void *)jb->s64.img_a
+                                                    : (const void *)jb->s32.img_a;
+        if (!jb->vol0 && cudaMallocAsync(&jb->vol0, bytes, st) != cudaSuccess) {
+            jb->vol0 = nullptr;
+            set_error("out of device memory for the initial volume");
+            rc = NUDIM_ENOMEM;
+        }
+        if (!rc && cudaMemcpyAsync(jb->vol0, src, bytes, cudaMemcpyDeviceToDevice, st) !=
+                       cudaSuccess) {
+            set_error("initial volume copy failed");
+            rc = NUDIM_ECUDA;
+        }
     }
     cleanup();
     if (!rc) {
@@ -875,11 +894,24 @@ int nudim_job_get_volume(nudim_job *jb, double *out, size_t n, int crop)
 int nudim_job_get_initial_volume(nudim_job *jb, double *out, size_t n)
 {
     if (!jb || !out) return NUDIM_EINVAL;
-    if (!jb->ready || jb->vol0.size() != n) {
+    const nudim_job_desc &d = jb->d;
+    size_t V = (size_t)d.np * d.np * d.nz;
+    if (!jb->ready || !jb->vol0 || n != V) {
         set_error("initial volume unavailable or wrong size");
         return jb->ready ? NUDIM_EINVAL : NUDIM_ESTATE;
     }
-    memcpy(out, jb->vol0.data(), sizeof(double) * n);
+    NUDIM_CUDA(cudaSetDevice(jb->ctx->device));
+    cudaStream_t st = jb->stream;
+    if (d.precision == NUDIM_FP64) {
+        NUDIM_CUDA(cudaMemcpyAsync(out, jb->vol0, sizeof(double) * V, cudaMemcpyDeviceToHost, st));
+    } else {
+        // widened in the state's CGNR scratch (V complex floats = V doubles of
+        // room), in stream order with the job's iterations
+        double *tmpd = (double *)jb->s32.z;
+        NUDIM_TRY(launch_to_double<float>((const float *)jb->vol0, tmpd, V, st));
+        NUDIM_CUDA(cudaMemcpyAsync(out, tmpd, sizeof(double) * V, cudaMemcpyDeviceToHost, st));
+    }
+    NUDIM_CUDA(cudaStreamSynchronize(st));
     return NUDIM_OK;
 }
 

@@ -141,3 +141,20 @@ def test_job_crop_and_state(gpu_ctx, orc, nudim_built):
     full, crop = job.volume(), job.volume(crop=True)
     assert np.array_equal(crop, full[:, 2:22, 2:22])
     job.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_initial_volume_kept_across_steps(gpu_ctx, orc, nudim_built, precision):
+    """The initial volume (recovered-0.txt) stays available after iterations
+    have overwritten the job's volume, in both forms."""
+    kw = dict(STABLE["er20_diffusion_weight"], ner=3)
+    proj = inputs_for(orc, kw)
+    job = nudim_built.Job(gpu_ctx, precision=precision, **kw)
+    job.set_projections(proj)
+    a = job.initial_volume()
+    job.step(3)
+    b = job.initial_volume()
+    job.close()
+    assert np.array_equal(a, b)
+    o0 = orc.reconstruct(proj, **kw)[0]
+    assert rel(a, o0) < (1e-9 if precision == 0 else 1e-4)
