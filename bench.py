@@ -519,7 +519,7 @@ def run_ours(args):
     peaks, peak_kind = load_peaks()
     c, r = workload_config()
     V = r["nz"] * r["np"] ** 2
-    ctx = ng.Context(local)
+    ctx = ng.Context(local, ng.CTX_AUTOTUNE if args.autotune else 0)
     vol, proj = make_inputs(ctx, CFG, seed=MASTER_SEED + rank, cfg=c)
 
     # ---- mixed form, device resident (the headline `value`)
@@ -610,6 +610,7 @@ def run_ours(args):
                 "Gaussian noise at SNR 0.5",
         "config": config_block(r),
         "form": "mixed (FP32 spreading/FFT/stencils, compensated gather, FP64 node/KB tables)",
+        "autotune": bool(args.autotune),
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "kernel_time_share": shares,
         "clocks": clk,
     }
@@ -697,6 +698,8 @@ def main():
     ap.add_argument("--serve-fp64", action="store_true", help="also serve the FP64 form")
     ap.add_argument("--nz", type=int, default=0,
                     help="override the number of Z-planes (small-case profiling only)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="context with NUDIM_CTX_AUTOTUNE (plan candidates timed per geometry)")
     ap.add_argument("--tv", default="",
                     help="NZxNYxNX: only time nudim_tv (40 inner iterations) on a volume of "
                          "that shape in both forms (a kernel micro-benchmark)")

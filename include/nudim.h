@@ -90,6 +90,12 @@ int nudim_abi_version(void);
 /* Context flags. */
 #define NUDIM_CTX_GRID_NFFT 1u /* NFFT through an n0 x n1 grid in HBM + cuFFT (cross-check
                                   path); the default keeps the grid on chip (fused) */
+#define NUDIM_CTX_AUTOTUNE 2u  /* the first fused NFFT plan of each geometry (N0, N1, M,
+                                  precision) times one trafo + adjoint for each trafo
+                                  column width and planes per spreading CTA and keeps
+                                  the fastest for the context's later plans; no
+                                  reference counterpart (NFFT3 plans have no such
+                                  choice) */
 
 /* Create a context on CUDA device `device`.  flags: 0 or NUDIM_CTX_* bits. */
 int nudim_ctx_create(int device, unsigned flags, nudim_ctx **out);
@@ -223,6 +229,9 @@ int nudim_project_dft(nudim_ctx *ctx, const double *density, int nx, int ny, int
 int nudim_nfft_plan_create(nudim_ctx *ctx, int N0, int N1, int M, const double *x,
                            int precision, nudim_nfft_plan **out);
 int nudim_nfft_plan_destroy(nudim_nfft_plan *plan);
+/* The plan's fused-path choice: trafo column-block width and Z-planes per
+ * spreading CTA (both 0 on the grid path).  No reference counterpart. */
+int nudim_nfft_plan_tuning(nudim_nfft_plan *plan, int *trafo_cols, int *spread_planes);
 
 /* nfft_trafo (reconstruction.c:361, 571) on `nplanes` planes:
  * f[p][j] = sum_k f_hat[p][k] exp(-2 pi i k.x_j); f_hat planes are N0*N1

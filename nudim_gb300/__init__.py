@@ -55,6 +55,7 @@ EXPORTS = [
     ("nudim_project_dft", _ip, [_vp, _dp, _ip, _ip, _ip, _ip, C.c_double, C.c_double,
                             C.c_double, C.c_double, C.c_ulong, _dp, _sz]),
     ("nudim_nfft_plan_create", _ip, [_vp, _ip, _ip, _ip, _dp, _ip, C.POINTER(_vp)]),
+    ("nudim_nfft_plan_tuning", _ip, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("nudim_nfft_plan_destroy", _ip, [_vp]),
     ("nudim_nfft_trafo", _ip, [_vp, _ip, _vp, _vp, _vp]),
     ("nudim_nfft_adjoint", _ip, [_vp, _ip, _vp, _vp, _vp]),
@@ -134,6 +135,7 @@ def footprint(**kw):
 
 
 CTX_GRID_NFFT = 1  # NFFT through an HBM grid + cuFFT (cross-check path)
+CTX_AUTOTUNE = 2   # time the fused plan's candidates per geometry, keep the fastest
 
 
 class Context:
@@ -315,6 +317,13 @@ class NfftPlan:
         _check(lib().nudim_nfft_plan_create(ctx.h, N0, N1, self.M, _dptr(x), precision,
                                             C.byref(h)))
         self.h = h
+
+    def tuning(self):
+        """(trafo column-block width, Z-planes per spreading CTA); (0, 0) on
+        the grid path."""
+        a, b = C.c_int(), C.c_int()
+        _check(lib().nudim_nfft_plan_tuning(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def trafo(self, nplanes, f_hat_ptr, f_ptr, stream=None):
         _check(lib().nudim_nfft_trafo(self.h, nplanes, f_hat_ptr, f_ptr, stream))

@@ -15,6 +15,7 @@
  *   --correct=<k>            MIXED: FP64 corrective iteration every k (0: off)
  *   --device=<n>             CUDA device (default 0)
  *   --fill=<file>            values for the unknown samples with --random
+ *   --autotune               time the NFFT plan candidates once, keep the fastest
  */
 #include <getopt.h>
 #include <math.h>
@@ -65,6 +66,7 @@ static void show_help(const char *s)
            "    --correct=<k>.            MIXED form: FP64 corrective iteration every k iterations.\n"
            "    --device=<n>.             CUDA device.\n"
            "    --fill=<file>.            Values of the unknown samples used with --random.\n"
+           "    --autotune.               Time the NFFT plan candidates once, keep the fastest.\n"
            "\n");
 }
 
@@ -105,7 +107,7 @@ int main(int argc, char *argv[])
     int nx = -1, nz = -1, nheight = -1, ncenter = -1, np = -1, nhio = -1, ner = -1;
     int config_denoise = 0, config_random = 0, config_weight = 0, config_print = 0,
         config_height = 0;
-    int precision = NUDIM_FP64, correct = 0, device = 0, denoise_m = -1;
+    int precision = NUDIM_FP64, correct = 0, device = 0, denoise_m = -1, autotune = 0;
 
     const struct option longopts[] = {
         {"help", 0, NULL, 'h'},       {"pad", 1, NULL, 'p'},      {"interval", 1, NULL, 't'},
@@ -120,7 +122,7 @@ int main(int argc, char *argv[])
         {"weight", 0, NULL, 16},
 #endif
         {"precision", 1, NULL, 20},   {"correct", 1, NULL, 21},   {"device", 1, NULL, 22},
-        {"fill", 1, NULL, 23},        {0, 0, NULL, 0}};
+        {"fill", 1, NULL, 23},        {"autotune", 0, NULL, 24},  {0, 0, NULL, 0}};
 
     while ((c = getopt_long(argc, argv, "hp:t:", longopts, NULL)) != -1) {
         switch (c) {
@@ -191,6 +193,7 @@ int main(int argc, char *argv[])
             if (*rval != '\0') { fprintf(stderr, "Invalid device!\n"); return 1; }
             break;
         case 23: fill_path = strdup(optarg); break;
+        case 24: autotune = 1; break;
         default: return 1;
         }
     }
@@ -275,7 +278,7 @@ int main(int argc, char *argv[])
 
     nudim_ctx *ctx;
     nudim_job *job;
-    int rc = nudim_ctx_create(device, 0, &ctx);
+    int rc = nudim_ctx_create(device, autotune ? NUDIM_CTX_AUTOTUNE : 0u, &ctx);
     if (rc) return fail("nudim_ctx_create", rc);
     rc = nudim_job_create(ctx, &d, &job);
     if (rc) return fail("nudim_job_create", rc);

@@ -533,6 +533,7 @@ int nudim_ctx_create(int device, unsigned flags, nudim_ctx **out)
     c->grid_budget = gb ? (size_t)atol(gb) << 20 : ((size_t)2 << 30);
     c->fused_budget = fused_budget_default();
     c->use_fused = !(flags & NUDIM_CTX_GRID_NFFT);
+    c->autotune = (flags & NUDIM_CTX_AUTOTUNE) != 0;
     *out = c;
     return NUDIM_OK;
 }
@@ -1170,6 +1171,15 @@ static int op_adjoint(NfftDev<T> &d, int nplanes, const void *f, void *fh, cudaS
 }
 
 extern "C" {
+int nudim_nfft_plan_tuning(nudim_nfft_plan *p, int *trafo_cols, int *spread_planes)
+{
+    if (!p || !trafo_cols || !spread_planes) return NUDIM_EINVAL;
+    bool f = p->prec == NUDIM_FP64 ? p->d64.fused : p->d32.fused;
+    *trafo_cols = !f ? 0 : p->prec == NUDIM_FP64 ? p->d64.BC : p->d32.BC;
+    *spread_planes = !f ? 0 : p->prec == NUDIM_FP64 ? p->d64.Pa : p->d32.Pa;
+    return NUDIM_OK;
+}
+
 int nudim_nfft_trafo(nudim_nfft_plan *p, int nplanes, const void *f_hat, void *f, void *stream)
 {
     if (!p || nplanes < 0 || (nplanes && (!f_hat || !f))) return NUDIM_EINVAL;

@@ -55,6 +55,10 @@ struct nudim_ctx {
     size_t grid_budget = 0;      // bytes a single NFFT pass may use for grids
     size_t fused_budget = 0;     // bytes of row spectra + partials per fused pass (L2 sized)
     bool use_fused = true;       // NFFT path: fused (default) or cuFFT grid path
+    // NUDIM_CTX_AUTOTUNE: the fused plan choice (trafo column width, planes per
+    // spreading CTA) found fastest for each (N0, N1, M, element size)
+    bool autotune = false;
+    std::map<std::tuple<int, int, int, int>, std::pair<int, int>> tuned;
     std::map<std::tuple<int, int, int, int>, cufftHandle> fft2d;  // n0,n1,batch,prec
     std::map<std::tuple<int, int, int, int>, cufftHandle> fftz;   // nz,P2,prec,kind
     double *scratch = nullptr;   // small reduction workspace (operator-level calls)
@@ -161,6 +165,9 @@ template <typename T> struct NfftDev {
     bool fused = false;
     int BC = 0, nblk = 0, smax = 0, rows = 4;    // trafo column blocks
     int BCa = 0, nblka = 0, nbands = 0, Pa = 1;  // adjoint column blocks, planes per CTA
+    // caps on the trafo column width and the planes per spreading CTA for
+    // init_fused (0: the defaults, or the NUDIM_TUNE_* environment knobs)
+    int tune_bc = 0, tune_planes = 0;
     size_t smem_col = 0, smem_row = 0, smem_spread = 0;
     C *tw0 = nullptr, *tw1 = nullptr;
     int *blk_off = nullptr, *ent = nullptr, *band_off = nullptr, *band_node = nullptr,
@@ -186,6 +193,7 @@ template <typename T> struct NfftDev {
     int adjoint(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca, cudaStream_t st);
 
     int init_fused(const NfftTables &t, cudaStream_t st);
+    int autotune(const NfftTables &t, cudaStream_t st);
     void release_fused();
     int fused_chunk(int nplanes) const;
     int trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia, cudaStream_t st);

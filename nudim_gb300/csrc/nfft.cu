@@ -208,6 +208,8 @@ int NfftDev<T>::init(nudim_ctx *c, const NfftTables &t, cudaStream_t st, Workspa
     bytes = nb_u + nb_p + sizeof(T) * (N0 + N1);
     // the fused path serves every geometry but extremely narrow grids, which
     // take the grid path below
+    if (c->use_fused && c->autotune && !tune_bc && !tune_planes)
+        NUDIM_TRY(autotune(t, st));
     if (c->use_fused && init_fused(t, st) == NUDIM_OK) return NUDIM_OK;
     fused = false;
     // grid path: tile lists of the spreading gather

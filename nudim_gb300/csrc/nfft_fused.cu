@@ -712,10 +712,12 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     int bc = (int)((128 << 10) / (2 * sizeof(C) * (size_t)t.n0));
     if (bc > 4) bc = 4;
     if (bc > t.n1) bc = t.n1;
-    // NUDIM_TUNE_BC caps the width (a tuning knob: narrower blocks fit more
-    // CTAs per SM at the cost of more (node, block) entries)
-    if (const char *e = getenv("NUDIM_TUNE_BC")) {
-        int v = atoi(e);
+    // the autotuner's cap, else NUDIM_TUNE_BC (a tuning knob: narrower blocks
+    // fit more CTAs per SM at the cost of more (node, block) entries)
+    {
+        int v = tune_bc;
+        if (!v)
+            if (const char *e = getenv("NUDIM_TUNE_BC")) v = atoi(e);
         if (v >= 1 && v < bc) bc = v;
     }
     int p = 1;
@@ -755,10 +757,12 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
                   : p == 2 ? spread_stage_bytes<T, 2>(Wa) : spread_stage_bytes<T, 1>(Wa);
         return (p + 1) * bufa + kSpreadWarps * st;
     };
-    // NUDIM_TUNE_PLANES caps the planes per CTA (a tuning knob)
+    // the autotuner's cap, else NUDIM_TUNE_PLANES, caps the planes per CTA
     Pa = 4;
-    if (const char *e = getenv("NUDIM_TUNE_PLANES")) {
-        int v = atoi(e);
+    {
+        int v = tune_planes;
+        if (!v)
+            if (const char *e = getenv("NUDIM_TUNE_PLANES")) v = atoi(e);
         if (v >= 1 && v < 4) Pa = v >= 2 ? 2 : 1;
     }
     while (Pa > 1 && spread_smem(Pa) > ((size_t)212 << 10)) Pa /= 2;
@@ -953,6 +957,95 @@ int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropAr
 
 template int NfftDev<double>::init_fused(const NfftTables &, cudaStream_t);
 template int NfftDev<float>::init_fused(const NfftTables &, cudaStream_t);
+
+// NUDIM_CTX_AUTOTUNE: for a geometry not yet tuned in this context, build the
+// fused plan for each trafo column width (4, 2) and planes per spreading CTA
+// (4, 2, 1), time one trafo + adjoint of a batch of planes for each (after one
+// untimed pair, CUDA events on the plan's stream), keep the fastest in the
+// context and use it for this plan.  Candidates that build the same plan as
+// an earlier one are not timed again.
+template <typename T> int NfftDev<T>::autotune(const NfftTables &t, cudaStream_t st)
+{
+    const auto key = std::make_tuple(t.N0, t.N1, t.M, (int)sizeof(T));
+    auto hit = ctx->tuned.find(key);
+    if (hit != ctx->tuned.end()) {
+        tune_bc = hit->second.first;
+        tune_planes = hit->second.second;
+        return NUDIM_OK;
+    }
+    const int nb = 16;  // planes per timed transform
+    void *fh = nullptr, *f = nullptr;
+    const size_t bh = sizeof(C) * (size_t)nb * t.N0 * t.N1, bf = sizeof(C) * (size_t)nb * t.M;
+    NUDIM_CUDA(cudaMallocAsync(&fh, bh, st));
+    NUDIM_CUDA(cudaMallocAsync(&f, bf, st));
+    NUDIM_CUDA(cudaMemsetAsync(fh, 0x3c, bh, st));
+    NUDIM_CUDA(cudaMemsetAsync(f, 0x3c, bf, st));
+    cudaEvent_t e0, e1;
+    NUDIM_CUDA(cudaEventCreate(&e0));
+    NUDIM_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    int choice_bc = 0, choice_p = 0, rc = NUDIM_OK;
+    std::vector<std::pair<int, int>> built;  // (BC, Pa) of the plans already timed
+    for (int bcc : {4, 2})
+        for (int pc : {4, 2, 1}) {
+            NfftDev<T> trial;
+            trial.tune_bc = bcc;
+            trial.tune_planes = pc;
+            if (trial.init(ctx, t, st, wsp) != NUDIM_OK || !trial.fused) {
+                trial.release();
+                continue;
+            }
+            const std::pair<int, int> got(trial.BC, trial.Pa);
+            bool seen = false;
+            for (auto &b : built) seen = seen || b == got;
+            if (!seen) {
+                built.push_back(got);
+                PadArgs<T> pa;
+                pa.src = fh;
+                pa.src_stride = (size_t)t.N0 * t.N1;
+                InterpArgs<T> ia;
+                ia.out = (C *)f;
+                ia.out_stride = t.M;
+                SpreadArgs<T> sa;
+                sa.f = (const C *)f;
+                sa.f_stride = t.M;
+                CropArgs<T> ca;
+                ca.out = (C *)fh;
+                ca.out_stride = (size_t)t.N0 * t.N1;
+                float ms = 0.f;
+                rc = trial.trafo(nb, pa, ia, st);
+                if (!rc) rc = trial.adjoint(nb, sa, ca, st);
+                if (!rc && cudaEventRecord(e0, st) != cudaSuccess) rc = NUDIM_ECUDA;
+                if (!rc) rc = trial.trafo(nb, pa, ia, st);
+                if (!rc) rc = trial.adjoint(nb, sa, ca, st);
+                if (!rc && (cudaEventRecord(e1, st) != cudaSuccess ||
+                            cudaEventSynchronize(e1) != cudaSuccess ||
+                            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+                    rc = NUDIM_ECUDA;
+                if (!rc && (choice_bc == 0 || ms < best)) {
+                    best = ms;
+                    choice_bc = bcc;
+                    choice_p = pc;
+                }
+            }
+            trial.release();
+            if (rc) break;
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(fh, st);
+    cudaFreeAsync(f, st);
+    if (rc) return rc;
+    if (choice_bc) {
+        ctx->tuned[key] = std::make_pair(choice_bc, choice_p);
+        tune_bc = choice_bc;
+        tune_planes = choice_p;
+    }
+    return NUDIM_OK;
+}
+
+template int NfftDev<double>::autotune(const NfftTables &, cudaStream_t);
+template int NfftDev<float>::autotune(const NfftTables &, cudaStream_t);
 template void NfftDev<double>::release_fused();
 template void NfftDev<float>::release_fused();
 template int NfftDev<double>::fused_chunk(int) const;

@@ -16,14 +16,20 @@ from gpu_util import cdtype, rel, to_dev
 pytestmark = pytest.mark.gpu
 
 
-def run(nudim_built, orc, env, P, prec, B=5):
+def run(nudim_built, orc, env, P, prec, B=5, flags=0, tuning=None):
     import torch
     old = {k: os.environ.get(k) for k in env}
     os.environ.update(env)
     try:
-        ctx = nudim_built.Context(0)
+        ctx = nudim_built.Context(0, flags)
         x = orc.polar_nodes(-60, 60, 2, 1, P)
         plan = nudim_built.NfftPlan(ctx, P, P, x, prec)
+        if tuning is not None:
+            tuning.append(plan.tuning())
+            # a second plan of the geometry takes the context's recorded choice
+            p2 = nudim_built.NfftPlan(ctx, P, P, x, prec)
+            tuning.append(p2.tuning())
+            p2.close()
         rng = np.random.default_rng(P + prec)
         fh = rng.standard_normal((B, P, P)) + 1j * rng.standard_normal((B, P, P))
         y = rng.standard_normal((B, len(x))) + 1j * rng.standard_normal((B, len(x)))
@@ -73,3 +79,19 @@ def test_one_column_blocks_fall_back_to_the_grid_path(nudim_built, orc, prec):
     tol = 1e-12 if prec == 0 else 2e-5
     assert rel(g, base[1]) < tol
     assert rel(f, base[0]) < tol
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_autotune_chooses_a_candidate_with_the_same_results(nudim_built, orc, prec):
+    """NUDIM_CTX_AUTOTUNE times the candidate plans and keeps one: its choice
+    is a valid (column width, planes per CTA) pair, later plans of the
+    geometry reuse it, and its results are those of the default plan to the
+    tolerances above (the adjoint exactly)."""
+    base = run(nudim_built, orc, {}, 96, prec)
+    tuning = []
+    f, g = run(nudim_built, orc, {}, 96, prec, flags=nudim_built.CTX_AUTOTUNE, tuning=tuning)
+    bc, planes = tuning[0]
+    assert bc in (2, 4) and planes in (1, 2, 4)
+    assert tuning[1] == tuning[0]
+    assert np.array_equal(g, base[1])
+    assert rel(f, base[0]) < (1e-14 if prec == 0 else 1e-6)
