@@ -166,6 +166,12 @@ int nudim_job_get_initial_volume(nudim_job *job, double *out, size_t n);
  * (reconstruction.c:603-604).  *count receives the number written. */
 int nudim_job_get_rfactor(nudim_job *job, double *hist, int cap, int *count);
 int nudim_job_iterations_done(nudim_job *job, int *done);
+/* Corrective FP64 iterations a NUDIM_MIXED job has run (desc.correct_every:
+ * every k-th iteration checks the measured-slice mismatch R of the current
+ * volume in FP32 and FP64 and runs the iteration in FP64 when they differ
+ * by more than the relative tolerance NUDIM_CORRECT_TOL (environment; 0, the
+ * default, corrects at every check).  No reference counterpart. */
+int nudim_job_corrections(nudim_job *job, int *count);
 /* Capture the volume before and after denoising at outer iteration `nn`
  * (the reference's grad_before/grad_after dumps).  Host buffers of
  * nz*np*np doubles each stay owned by the caller; pass nn < 0 to disable. */

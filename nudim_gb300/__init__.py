@@ -43,6 +43,7 @@ EXPORTS = [
     ("nudim_job_get_volume", _ip, [_vp, _dp, _sz, _ip]),
     ("nudim_job_get_initial_volume", _ip, [_vp, _dp, _sz]),
     ("nudim_job_get_rfactor", _ip, [_vp, _dp, _ip, C.POINTER(_ip)]),
+    ("nudim_job_corrections", _ip, [_vp, C.POINTER(C.c_int)]),
     ("nudim_job_iterations_done", _ip, [_vp, C.POINTER(_ip)]),
     ("nudim_job_set_denoise_dump", _ip, [_vp, _ip, _dp, _dp]),
     ("nudim_server_create", _ip, [_vp, _sz, _ip, C.POINTER(_vp)]),
@@ -238,6 +239,12 @@ class Job:
     def done(self):
         v = C.c_int()
         _check(lib().nudim_job_iterations_done(self.h, C.byref(v)))
+        return v.value
+
+    def corrections(self):
+        """Corrective FP64 iterations run so far (NUDIM_MIXED with correct_every)."""
+        v = C.c_int()
+        _check(lib().nudim_job_corrections(self.h, C.byref(v)))
         return v.value
 
     def set_denoise_dump(self, nn):

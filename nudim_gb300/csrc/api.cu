@@ -155,6 +155,7 @@ struct nudim_job {
     // the initial volume (reconstruction.c:521-540, recovered-0.txt) kept on
     // the device in the job's precision; sent to the host only on request
     void *vol0 = nullptr;
+    int corrections = 0;  // corrective FP64 iterations run
 };
 
 struct nudim_nfft_plan {
@@ -404,6 +405,63 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
         if (g) cudaGraphDestroy(g);
         cudaGetLastError();  // a failed capture leaves eager execution in place
     }
+    return NUDIM_OK;
+}
+
+// The measured-slice mismatch R of the state's current volume (the first
+// steps of an iteration: pack, forward Z-FFT, trafo with the constraint
+// epilogue, reconstruction.c:548-582); R lands in rh[nn], which the iteration
+// that follows rewrites.
+template <typename T> static int state_residual(nudim_job *jb, JobState<T> &s, int nn)
+{
+    cudaStream_t st = jb->stream;
+    const nudim_job_desc &d = jb->d;
+    const int nz = d.nz, np = d.np, M = jb->M;
+    const size_t P2 = (size_t)np * np;
+    NUDIM_TRY(launch_set_counter(s.it, nn, st));
+    NUDIM_TRY(launch_pack<T>(s.img_a, s.data, nz, P2, st));
+    NUDIM_TRY(zfft<T>(jb, s, CUFFT_FORWARD));
+    PadArgs<T> pa;
+    pa.src = s.data;
+    pa.src_stride = P2;
+    InterpArgs<T> ia;
+    ia.mode = IM_CONSTRAINT;
+    ia.out = s.y;
+    ia.out_stride = M;
+    ia.s = s.slices;
+    ia.s_stride = M;
+    ia.known = s.known;
+    ia.line_len = np;
+    ia.part = s.part;
+    ia.part_stride = s.part_stride;
+    NUDIM_TRY(s.pl.trafo(nz, pa, ia, st));
+    return launch_finish_r<T>(s.part, s.pl.interp_blocks(), nz, s.part_stride, s.rh, s.it, st);
+}
+
+// NUDIM_CORRECT_TOL: relative difference between the FP32 and the FP64 R of
+// the current volume above which the periodic check runs the corrective FP64
+// iteration; 0 (the default) runs it at every check.
+static double correct_tol()
+{
+    const char *e = getenv("NUDIM_CORRECT_TOL");
+    double v = e ? atof(e) : 0.0;
+    return v > 0 ? v : 0.0;
+}
+
+// The periodic FP64 residual check of a mixed job: R of the current volume in
+// both forms; *need = their relative difference exceeds tol.
+static int residual_check(nudim_job *jb, int nn, double tol, bool *need)
+{
+    cudaStream_t st = jb->stream;
+    size_t V = (size_t)jb->d.np * jb->d.np * jb->d.nz;
+    NUDIM_TRY(launch_to_double<float>(jb->s32.img_a, jb->s64.img_a, V, st));
+    NUDIM_TRY(state_residual<double>(jb, jb->s64, nn));
+    NUDIM_TRY(state_residual<float>(jb, jb->s32, nn));
+    double r64 = 0, r32 = 0;
+    NUDIM_CUDA(cudaMemcpyAsync(&r64, jb->s64.rh + nn, sizeof(double), cudaMemcpyDeviceToHost, st));
+    NUDIM_CUDA(cudaMemcpyAsync(&r32, jb->s32.rh + nn, sizeof(double), cudaMemcpyDeviceToHost, st));
+    NUDIM_CUDA(cudaStreamSynchronize(st));
+    *need = !(fabs(r32 - r64) <= tol * fabs(r64));
     return NUDIM_OK;
 }
 
@@ -850,7 +908,15 @@ int nudim_step(nudim_ctx *ctx, nudim_job *const *jobs, int njobs, int iters)
             if (jb->d.precision == NUDIM_FP64) {
                 NUDIM_TRY(state_iterate<double>(jb, jb->s64, nn));
             } else if (jb->d.correct_every > 0 && (nn + 1) % jb->d.correct_every == 0) {
-                NUDIM_TRY(corrective_iteration(jb, nn));
+                const double tol = correct_tol();
+                bool need = true;
+                if (tol > 0) NUDIM_TRY(residual_check(jb, nn, tol, &need));
+                if (need) {
+                    NUDIM_TRY(corrective_iteration(jb, nn));
+                    jb->corrections++;
+                } else {
+                    NUDIM_TRY(state_iterate<float>(jb, jb->s32, nn));
+                }
             } else {
                 NUDIM_TRY(state_iterate<float>(jb, jb->s32, nn));
             }
@@ -934,6 +1000,13 @@ int nudim_job_iterations_done(nudim_job *jb, int *done)
 {
     if (!jb || !done) return NUDIM_EINVAL;
     *done = jb->done;
+    return NUDIM_OK;
+}
+
+int nudim_job_corrections(nudim_job *jb, int *count)
+{
+    if (!jb || !count) return NUDIM_EINVAL;
+    *count = jb->corrections;
     return NUDIM_OK;
 }
 

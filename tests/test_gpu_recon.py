@@ -158,3 +158,33 @@ def test_initial_volume_kept_across_steps(gpu_ctx, orc, nudim_built, precision):
     assert np.array_equal(a, b)
     o0 = orc.reconstruct(proj, **kw)[0]
     assert rel(a, o0) < (1e-9 if precision == 0 else 1e-4)
+
+
+def _mixed_run(nudim_built, ctx, proj, kw, correct_every):
+    job = nudim_built.Job(ctx, precision=1, correct_every=correct_every, **kw)
+    job.set_projections(proj)
+    job.step(kw["nhio"] + kw["ner"])
+    out = job.volume(), job.corrections()
+    job.close()
+    return out
+
+
+def test_residual_check_triggers_the_fp64_iteration(gpu_ctx, orc, nudim_built, monkeypatch):
+    """correct_every = 4 checks R of the current volume in FP32 and FP64 at
+    every 4th iteration.  Tolerance 0 (default): every check corrects.  A huge
+    tolerance: no check corrects and the job is the plain mixed one, bit for
+    bit.  A tolerance below any FP32/FP64 difference: every check corrects,
+    bit for bit as with tolerance 0."""
+    kw = dict(STABLE["er20_diffusion_weight"], nhio=4, ner=8)
+    proj = inputs_for(orc, kw)
+    monkeypatch.delenv("NUDIM_CORRECT_TOL", raising=False)
+    v_all, n_all = _mixed_run(nudim_built, gpu_ctx, proj, kw, 4)
+    assert n_all == 3
+    plain, n_plain = _mixed_run(nudim_built, gpu_ctx, proj, kw, 0)
+    assert n_plain == 0
+    monkeypatch.setenv("NUDIM_CORRECT_TOL", "1e30")
+    v_none, n_none = _mixed_run(nudim_built, gpu_ctx, proj, kw, 4)
+    assert n_none == 0 and np.array_equal(v_none, plain)
+    monkeypatch.setenv("NUDIM_CORRECT_TOL", "1e-15")
+    v_tiny, n_tiny = _mixed_run(nudim_built, gpu_ctx, proj, kw, 4)
+    assert n_tiny == 3 and np.array_equal(v_tiny, v_all)
