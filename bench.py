@@ -197,7 +197,7 @@ def timed_steps(ctx, job, steps, nvtx=None):
 # DRAM bytes per Z-plane of the adjoint NFFT's two kernels, from ncu captures of
 # 32-plane launches on the same geometry (profiles/spread_colifft_cfg2_32planes.md,
 # which lists both): dram__bytes_read.sum + dram__bytes_write.sum / 32.
-MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((77.919488e6 + 71.974400e6)      # k_spread_colifft
+MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((75.449856e6 + 71.426048e6)      # k_spread_colifft
                                       + (100.737792e6 + 36.037120e6)) / 32  # k_rowifft_crop
 
 
