@@ -57,6 +57,7 @@ def run(exe, *args, cwd=None):
 def test_cli_help(nudim_built):
     r = run("reconstruction", "-h")
     assert r.returncode == 0 and "--padangle" in r.stdout and "--center" in r.stdout
+    assert "--autotune" in r.stdout
     r = run("reconstruction_parallel", "--help")
     assert r.returncode == 0 and "--center" not in r.stdout
     r = run("projection_sim", "-h")

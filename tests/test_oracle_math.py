@@ -177,3 +177,20 @@ def test_project_dft_matches_2d1d_with_the_true_pi(orc, shape, npx, rng_):
     assert rel(exact, a) < 1e-11
     ref_pi = orc.project_dft(vol, npx, *rng_)
     assert 1e-9 < rel(ref_pi, exact) < 1e-5
+
+
+def test_3d_nodes_are_the_2d_table_with_z(orc):
+    """grid_slice_3D's (r cos g, r sin g) equal the 2D table's entries
+    (stored as (r sin g, r cos g)) bit for bit, and its Z by repeated
+    addition matches the uniform Z nodes; the DFT method's device code builds
+    its per-axis phases from the 2D table on that basis."""
+    np_, nz = 24, 10
+    x3 = orc.nodes_3d(-60, 60, 15, np_, nz)
+    x2 = orc.equal_angle_sample_2d(-60, 60, 15, np_).reshape(x3.shape[0], np_, 2)
+    for j in range(nz):
+        assert np.array_equal(x3[:, j, :, 0], x2[:, :, 1])
+        assert np.array_equal(x3[:, j, :, 1], x2[:, :, 0])
+    z0 = -0.5 - 1.0 / nz
+    for j in range(nz):
+        z0 += 1.0 / nz
+        assert np.all(x3[:, j, :, 2] == z0)
