@@ -3,8 +3,10 @@ build_fused_lists) on the CPU: every node's trafo entries (per column block)
 and adjoint tile entries (per R x BCa tile) must reproduce exactly its window
 weights psi0[r - u0] * psi1[c - u1] on its 14 x 14 window of the oversampled
 grid (wrapping at the edges), each grid point once; tile lists are in
-ascending node order and each block's tiles ordered longest first.  A g++
-harness links tables.cpp directly (no GPU)."""
+ascending node order and each block's tiles ordered longest first.  The grid
+path's spreading tile lists (build_tile_lists) hold, per tile, exactly the
+nodes whose window meets it, ascending.  A g++ harness links tables.cpp
+directly (no GPU)."""
 import os
 import shutil
 import subprocess
@@ -115,8 +117,44 @@ static int check(int N, int M, int BC, bool pair_rows, unsigned seed)
     return 0;
 }
 
+// grid path: per ty x tx tile, the nodes whose window meets it, ascending
+static int check_tiles(int N, int M, unsigned seed)
+{
+    std::mt19937 g(seed);
+    std::uniform_real_distribution<double> U(-0.5, 0.5);
+    std::vector<double> x(2 * (size_t)M);
+    for (auto &v : x) v = U(g);
+    x[0] = -0.5; x[1] = 0.5 - 1e-9;
+    NfftTables t;
+    if (build_nfft_tables(N, N, M, x.data(), 16, 16, &t)) return 60;
+    std::vector<int> off, nodes;
+    build_tile_lists(t, &off, &nodes);
+    const int n0 = t.n0, n1 = t.n1, ty = t.ty, tx = t.tx;
+    const int nty = (n0 + ty - 1) / ty, ntx = (n1 + tx - 1) / tx;
+    if ((int)off.size() != nty * ntx + 1) return 61;
+    for (int a = 0; a < nty; a++)
+        for (int b = 0; b < ntx; b++) {
+            int tile = a * ntx + b;
+            std::vector<int> want;
+            for (int j = 0; j < M; j++) {
+                bool hit = false;
+                for (int s = 0; s < kWin && !hit; s++)
+                    for (int u = 0; u < kWin && !hit; u++) {
+                        int r = (t.u0[j] + s) & (n0 - 1), c = (t.u1[j] + u) & (n1 - 1);
+                        hit = r / ty == a && c / tx == b;
+                    }
+                if (hit) want.push_back(j);
+            }
+            std::vector<int> got(nodes.begin() + off[tile], nodes.begin() + off[tile + 1]);
+            if (got != want) return 62;
+        }
+    return 0;
+}
+
 int main()
 {
+    if (int r = check_tiles(24, 200, 7)) { std::printf("tiles %d\n", r); return 1; }
+    if (int r = check_tiles(56, 300, 8)) { std::printf("tiles %d\n", r); return 1; }
     struct Case { int N, M, BC; bool pair; unsigned seed; };
     const Case cases[] = {{24, 300, 4, true, 1}, {24, 300, 2, true, 2}, {40, 500, 4, false, 3},
                           {8, 60, 16, true, 4}, {96, 400, 4, true, 5}};
