@@ -11,9 +11,16 @@ SNR 0.5, reconstructed at np = nx = 384, nz = 256, padangle 1, 50 HIO + 50
 ER, anisotropic-diffusion denoise.  `value` is the mixed form (FP32
 spreading/FFT/stencils, FP64 tables), inputs resident in HBM; `e2e` is the
 same metric through the C ABI with host buffers (tilt series in, volume out,
-setup included); `fp64_plain` is the FP64 form on the same job.
+setup included); `fp64_plain` is the FP64 form on the same job.  Further
+legs on the same line: `batched` (48 uneven TV jobs stepped together, one
+stream each), `serving` (Poisson arrivals into the continuous-batching
+server, p50/p99 latency), `cpu_baseline` (the oracle port on the host cores,
+a bounded sample), and with --large the 768^2 x 256 TV configuration with
+its FP64 correction.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+       [--large] [--batch-jobs J] [--serve-jobs J] [--autotune]
+       python bench.py --tv NZxNYxNX      (the TV kernels alone)
 Under torchrun each rank runs an independent replica on its own GPU
 (the path has no cross-rank exchange): value = all ranks' voxel-iterations
 / max rank time.
