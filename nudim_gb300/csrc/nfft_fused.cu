@@ -976,18 +976,21 @@ template <typename T> int NfftDev<T>::autotune(const NfftTables &t, cudaStream_t
     const int nb = 16;  // planes per timed transform
     void *fh = nullptr, *f = nullptr;
     const size_t bh = sizeof(C) * (size_t)nb * t.N0 * t.N1, bf = sizeof(C) * (size_t)nb * t.M;
-    NUDIM_CUDA(cudaMallocAsync(&fh, bh, st));
-    NUDIM_CUDA(cudaMallocAsync(&f, bf, st));
-    NUDIM_CUDA(cudaMemsetAsync(fh, 0x3c, bh, st));
-    NUDIM_CUDA(cudaMemsetAsync(f, 0x3c, bf, st));
-    cudaEvent_t e0, e1;
-    NUDIM_CUDA(cudaEventCreate(&e0));
-    NUDIM_CUDA(cudaEventCreate(&e1));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = NUDIM_OK;
+    if (cudaMallocAsync(&fh, bh, st) != cudaSuccess || cudaMallocAsync(&f, bf, st) != cudaSuccess ||
+        cudaMemsetAsync(fh, 0x3c, bh, st) != cudaSuccess ||
+        cudaMemsetAsync(f, 0x3c, bf, st) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess) {
+        set_error("autotune: device allocation failed");
+        rc = NUDIM_ENOMEM;
+    }
     float best = 0.f;
-    int choice_bc = 0, choice_p = 0, rc = NUDIM_OK;
+    int choice_bc = 0, choice_p = 0;
     std::vector<std::pair<int, int>> built;  // (BC, Pa) of the plans already timed
     for (int bcc : {4, 2})
         for (int pc : {4, 2, 1}) {
+            if (rc) break;
             NfftDev<T> trial;
             trial.tune_bc = bcc;
             trial.tune_planes = pc;
@@ -1031,10 +1034,10 @@ template <typename T> int NfftDev<T>::autotune(const NfftTables &t, cudaStream_t
             trial.release();
             if (rc) break;
         }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFreeAsync(fh, st);
-    cudaFreeAsync(f, st);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (fh) cudaFreeAsync(fh, st);
+    if (f) cudaFreeAsync(f, st);
     if (rc) return rc;
     if (choice_bc) {
         ctx->tuned[key] = std::make_pair(choice_bc, choice_p);
