@@ -78,7 +78,10 @@ typedef struct nudim_job_desc {
     int variant;            /* enum nudim_variant */
     int precision;          /* enum nudim_precision */
     int cgnr_iters;         /* CGNR steps per plane (reference: 10; 0 -> 10) */
-    int correct_every;      /* NUDIM_MIXED: FP64 residual check period (0: never) */
+    int correct_every;      /* NUDIM_MIXED: k > 0, every k-th iteration is an FP64
+                               residual check / corrective iteration; k < 0, every
+                               HIO iteration runs in FP64 (from the FP64 initial
+                               inverse) and only ER iterations in FP32; 0: never */
 } nudim_job_desc;
 
 /* ------------------------------------------------------------------ */
@@ -147,7 +150,11 @@ int nudim_job_set_projections(nudim_job *job, const double *proj, size_t n);
  * and never passes nhio+ner.  Iterations are queued round-robin over the
  * jobs, each on its own stream, so they overlap on the device; the call
  * returns when the work is queued (sync with nudim_job_sync, nudim_ctx_sync
- * or by reading results). */
+ * or by reading results).  A NUDIM_MIXED job's check iteration (see
+ * nudim_job_corrections; NUDIM_CORRECT_TOL > 0) first queues the residual
+ * check and is itself queued once the check's result reaches the host: the
+ * other jobs' iterations are queued meanwhile, and the call waits on the host
+ * only when every iteration it has left waits on a check. */
 int nudim_step(nudim_ctx *ctx, nudim_job *const *jobs, int njobs, int iters);
 /* Wait for all queued work of every job on the context's device. */
 int nudim_ctx_sync(nudim_ctx *ctx);
@@ -166,11 +173,13 @@ int nudim_job_get_initial_volume(nudim_job *job, double *out, size_t n);
  * (reconstruction.c:603-604).  *count receives the number written. */
 int nudim_job_get_rfactor(nudim_job *job, double *hist, int cap, int *count);
 int nudim_job_iterations_done(nudim_job *job, int *done);
-/* Corrective FP64 iterations a NUDIM_MIXED job has run (desc.correct_every:
+/* FP64 iterations a NUDIM_MIXED job has run (desc.correct_every = k > 0:
  * every k-th iteration checks the measured-slice mismatch R of the current
  * volume in FP32 and FP64 and runs the iteration in FP64 when they differ
  * by more than the relative tolerance NUDIM_CORRECT_TOL (environment; 0, the
- * default, corrects at every check).  No reference counterpart. */
+ * default, corrects at every check); k < 0: every HIO iteration).
+ * Consecutive FP64 iterations keep the volume in FP64.  No reference
+ * counterpart. */
 int nudim_job_corrections(nudim_job *job, int *count);
 /* Capture the volume before and after denoising at outer iteration `nn`
  * (the reference's grad_before/grad_after dumps).  Host buffers of
@@ -267,14 +276,17 @@ int nudim_tv(nudim_ctx *ctx, int precision, void *vol, int nz, int ny, int nx, f
  * manager owns the whole device, or a loop that must avoid the implicit
  * synchronisation of cudaMalloc/cudaFree).  Same semantics and kernels as
  * nudim_tv on the current CUDA device; the scratch (gradient field and sums)
- * is one fixed 32 MiB device array inside this library, present on every
- * GPU that loads it until the process exits: a volume needs
- * 8*(2*ceil(nz*ny*nx/256)+6) bytes (rounded up to 256) plus one real per
- * voxel, so FP64 volumes up to about 4.1 million voxels (FP32 about 8.2
- * million) fit; larger ones return NUDIM_EINVAL.  The first call on a device
- * looks up the array's device address; make that first call before any
- * stream capture.  All calls share the array: calls whose work overlaps on a
- * GPU race and must be serialised by the caller. */
+ * is one fixed 32 MiB (33554432-byte) device array inside this library,
+ * present on every GPU that loads it until the process exits.  A volume
+ * needs round_up(8 * (K + 4), 256) + S * nz*ny*nx bytes of it, with
+ * K = 2 * ceil(nx/32) * ceil(ny/16) * nz + 2 partial sums and S = 8 (FP64)
+ * or 4 (FP32); for planes that are whole 32 x 16 tiles that is about
+ * 4.1 million FP64 or 8.3 million FP32 voxels (e.g. FP32 127 x 256 x 256),
+ * while thin planes (nx or ny far below a tile) need far more partial sums
+ * per voxel.  Larger volumes return NUDIM_EINVAL.  The first call in each
+ * CUDA context on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * whose work overlaps on a GPU race and must be serialised by the caller. */
 int nudim_tv_noalloc(int precision, void *vol, int nz, int ny, int nx, float lam, int niter,
                      int height, int nheight, int ncenter, void *stream);
 

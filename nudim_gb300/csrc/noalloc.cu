@@ -24,11 +24,58 @@ constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch per device.  In host code the array's
-// name is only a host-side handle, never a device address, so the address
-// is looked up once per device (with that device current) and cached.
+// Device address of g_noalloc_scratch in the CUDA context current on the
+// calling thread.  In host code the array's name is only a host-side handle,
+// never a device address, so the address is looked up with
+// cudaGetSymbolAddress, with that device and context current, the first
+// time a context uses the array, and cached per device together with the
+// context's process-unique ID (cuCtxGetId).  A call from another context on
+// the same device -- after cudaDeviceReset, or from a driver-API or green
+// context -- has another ID and looks the address up again, so a stale
+// address is never handed to a kernel.  The two driver calls are reached
+// through cudaGetDriverEntryPointByVersion, so the library does not link
+// libcuda directly.
+typedef int (*ctx_get_current_fn)(void **ctx);
+typedef int (*ctx_get_id_fn)(void *ctx, unsigned long long *id);
+
+struct NoAllocSlot {
+    unsigned long long ctx_id = 0;
+    bool set = false;
+    void *addr = nullptr;
+};
+
 static std::mutex g_noalloc_mu;
-static void *g_noalloc_addr[128];
+static NoAllocSlot g_noalloc_slot[128];
+static ctx_get_current_fn g_ctx_current = nullptr;
+static ctx_get_id_fn g_ctx_id = nullptr;
+
+static int driver_entry(const char *name, void **fn)
+{
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    cudaError_t e = cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess) return cuda_fail(e, name, __FILE__, __LINE__);
+    if (q != cudaDriverEntryPointSuccess || !*fn) {
+        set_error("nudim_tv_noalloc: driver entry point %s unavailable", name);
+        return NUDIM_ECUDA;
+    }
+    return NUDIM_OK;
+}
+
+// The ID of the context current on this thread (0 when none is current yet).
+static int current_ctx_id(unsigned long long *id)
+{
+    void *cu = nullptr;
+    *id = 0;
+    if (g_ctx_current(&cu) != 0) {
+        set_error("nudim_tv_noalloc: cuCtxGetCurrent failed");
+        return NUDIM_ECUDA;
+    }
+    if (cu && g_ctx_id(cu, id) != 0) {
+        set_error("nudim_tv_noalloc: cuCtxGetId failed");
+        return NUDIM_ECUDA;
+    }
+    return NUDIM_OK;
+}
 
 static int noalloc_scratch(int dev, void **out)
 {
@@ -37,13 +84,23 @@ static int noalloc_scratch(int dev, void **out)
         set_error("device index %d out of range", dev);
         return NUDIM_EINVAL;
     }
-    if (!g_noalloc_addr[dev]) {
+    if (!g_ctx_current) NUDIM_TRY(driver_entry("cuCtxGetCurrent", (void **)&g_ctx_current));
+    if (!g_ctx_id) NUDIM_TRY(driver_entry("cuCtxGetId", (void **)&g_ctx_id));
+    unsigned long long id = 0;
+    NUDIM_TRY(current_ctx_id(&id));
+    NoAllocSlot &s = g_noalloc_slot[dev];
+    if (!s.set || id == 0 || s.ctx_id != id) {
+        // set-up for this device and context (makes the runtime's primary
+        // context current when no context was current yet)
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress", __FILE__, __LINE__);
-        g_noalloc_addr[dev] = p;
+        NUDIM_TRY(current_ctx_id(&id));
+        s.addr = p;
+        s.ctx_id = id;
+        s.set = id != 0;
     }
-    *out = g_noalloc_addr[dev];
+    *out = s.addr;
     return NUDIM_OK;
 }
 
