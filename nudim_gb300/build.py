@@ -24,6 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["nfft.cu", "nfft_fused.cu", "ops.cu", "denoise.cu", "api.cu", "serve.cu",
               "noalloc.cu", "project_dft.cu"]
 CXX_SOURCES = ["tables.cpp"]
+# CUDA executables beside the library (measurement helpers, no libnudim)
+CU_BIN = {"fp64_peak": "csrc/peak_fp64.cu"}
 CLI = {
     "reconstruction": ["cli/reconstruction.c", "cli/textio.c"],
     "reconstruction_parallel": ["cli/reconstruction.c", "cli/textio.c"],
@@ -84,6 +86,10 @@ def build(verbose=False, force=False):
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcufft",
               "-L" + os.path.join(cuda, "lib64")])
     os.makedirs(BIN, exist_ok=True)
+    for name, src in CU_BIN.items():
+        path, exe = os.path.join(PKG, src), os.path.join(BIN, name)
+        if force or _stale(exe, [path]):
+            _run([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", path, "-o", exe])
     for name, srcs in CLI.items():
         paths = [os.path.join(PKG, s) for s in srcs]
         if not all(os.path.exists(p) for p in paths):

@@ -7,7 +7,11 @@
 // admitted jobs -- at most two in flight per job, so a new arrival joins the
 // rotation within two rounds -- and, when a job's last iteration has run,
 // copies its volume to the host, records arrival-to-result latency and frees
-// its memory for the next admission.  Jobs run on separate streams, so their
+// its memory for the next admission.  A mixed job whose next iteration waits
+// on its periodic FP64 residual check is passed over until the check's
+// result has reached the host, so a check never stalls the other jobs or
+// admission.  Every CUDA status the loop sees other than "not ready" ends
+// the request with NUDIM_ECUDA and its message.  Jobs run on separate streams, so their
 // kernels overlap on the device; results do not depend on the mix (every
 // kernel is deterministic and a job's work stays on its stream).
 #include <algorithm>
@@ -73,6 +77,16 @@ struct nudim_server {
 
 namespace {
 
+// A request whose work failed: keep the first status and its message (the
+// worker thread's error text is overwritten by later calls).
+void fail(Request *r, int rc)
+{
+    if (r->rc != NUDIM_OK) return;
+    r->rc = rc;
+    r->err = last_error();
+    r->enqueued = r->d.nhio + r->d.ner;
+}
+
 void finish(nudim_server *s, Request *r, int rc)
 {
     if (r->job) {
@@ -80,8 +94,8 @@ void finish(nudim_server *s, Request *r, int rc)
             size_t V = (size_t)r->d.nz * r->d.np * r->d.np;
             r->vol.resize(V);
             rc = nudim_job_get_volume(r->job, r->vol.data(), V, 0);
+            if (rc) r->err = last_error();
         }
-        if (rc) r->err = last_error();
         nudim_job_destroy(r->job);
         r->job = nullptr;
     }
@@ -109,8 +123,11 @@ int admit(nudim_server *s, Request *r)
     int rc = nudim_job_create(s->ctx, &r->d, &r->job);
     if (!rc) rc = nudim_job_set_projections(r->job, r->proj.data(), r->proj.size());
     for (cudaEvent_t &e : r->ev)
-        if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
-            rc = NUDIM_ECUDA;
+        if (!rc) {
+            cudaError_t ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+            if (ce != cudaSuccess) rc = cuda_fail(ce, "serving: cudaEventCreate", __FILE__, __LINE__);
+        }
+    if (rc) r->err = last_error();
     return rc;
 }
 
@@ -159,24 +176,41 @@ void worker_main(nudim_server *s)
             if (r->enqueued >= total) continue;
             cudaEvent_t &slot = r->ev[r->enqueued & 1];
             // at most two iterations in flight per job
-            if (r->enqueued >= 2 && cudaEventQuery(slot) != cudaSuccess) continue;
-            nudim_job *j = r->job;
-            int rc = nudim_step(s->ctx, &j, 1, 1);
+            if (r->enqueued >= 2) {
+                cudaError_t q = cudaEventQuery(slot);
+                if (q == cudaErrorNotReady) continue;
+                if (q != cudaSuccess) {
+                    fail(r, cuda_fail(q, "serving: iteration event", __FILE__, __LINE__));
+                    continue;
+                }
+            }
+            bool issued = false;
+            int rc = job_try_step(r->job, &issued);
             if (rc) {
-                r->enqueued = total;
-                r->rc = rc;
+                fail(r, rc);
                 continue;
             }
-            cudaEventRecord(slot, (cudaStream_t)nudim_job_stream(r->job));
+            if (!issued) continue;  // waits on its residual check
+            cudaError_t e = cudaEventRecord(slot, (cudaStream_t)nudim_job_stream(r->job));
+            if (e != cudaSuccess) {
+                fail(r, cuda_fail(e, "serving: cudaEventRecord", __FILE__, __LINE__));
+                continue;
+            }
             r->enqueued++;
             progress = true;
         }
         // ---- completions
         for (Request *r : act) {
             int total = r->d.nhio + r->d.ner;
-            bool done = r->enqueued >= total &&
-                        (r->rc || total == 0 ||
-                         cudaEventQuery(r->ev[(r->enqueued - 1) & 1]) == cudaSuccess);
+            bool done = r->rc != NUDIM_OK || total == 0;
+            if (!done && r->enqueued >= total) {
+                cudaError_t q = cudaEventQuery(r->ev[(r->enqueued - 1) & 1]);
+                if (q == cudaSuccess) done = true;
+                else if (q != cudaErrorNotReady) {
+                    fail(r, cuda_fail(q, "serving: iteration event", __FILE__, __LINE__));
+                    done = true;
+                }
+            }
             if (!done) continue;
             {
                 std::lock_guard<std::mutex> lk(s->mu);

@@ -188,3 +188,36 @@ def test_residual_check_triggers_the_fp64_iteration(gpu_ctx, orc, nudim_built, m
     monkeypatch.setenv("NUDIM_CORRECT_TOL", "1e-15")
     v_tiny, n_tiny = _mixed_run(nudim_built, gpu_ctx, proj, kw, 4)
     assert n_tiny == 3 and np.array_equal(v_tiny, v_all)
+
+
+def test_fp64_hio_schedule(gpu_ctx, orc, nudim_built):
+    """correct_every < 0: a mixed job runs its HIO iterations in FP64 from the
+    FP64 initial inverse (the FP64 form's own iterations, bit for bit) and only
+    its ER iterations in FP32; consecutive FP64 iterations keep the volume in
+    FP64."""
+    kw = dict(STABLE["hio3_er3_diffusion_weight"], ner=0)
+    proj = inputs_for(orc, kw)
+    v64, rh64, _ = run_gpu(gpu_ctx, nudim_built, proj, **kw)
+    job = nudim_built.Job(gpu_ctx, precision=1, correct_every=-1, **kw)
+    job.set_projections(proj)
+    job.step(kw["nhio"])
+    assert job.corrections() == kw["nhio"]
+    assert np.array_equal(job.volume(), v64)
+    assert np.array_equal(job.rfactor(), rh64)
+    job.close()
+    kw = STABLE["hio3_er3_diffusion_weight"]
+    v64, _, _ = run_gpu(gpu_ctx, nudim_built, proj, **kw)
+    vm, _, _ = run_gpu(gpu_ctx, nudim_built, proj, precision=1, correct_every=-1, **kw)
+    assert rel(vm, v64) < 1e-5
+
+
+def test_consecutive_fp64_iterations_stay_fp64(gpu_ctx, orc, nudim_built):
+    """correct_every = 1: every iteration is FP64 and the volume is never
+    rounded to FP32 between them, so the job differs from the FP64 form only by
+    its FP32 initial inverse (FP32-sized differences, not amplified by ER)."""
+    kw = dict(STABLE["er20_diffusion_weight"], ner=4)
+    proj = inputs_for(orc, kw)
+    v64, rh64, _ = run_gpu(gpu_ctx, nudim_built, proj, **kw)
+    vc, rhc, _ = run_gpu(gpu_ctx, nudim_built, proj, precision=1, correct_every=1, **kw)
+    assert rel(vc, v64) < 1e-4
+    assert np.allclose(rhc, rh64, rtol=1e-4)
