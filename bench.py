@@ -201,19 +201,21 @@ def timed_steps(ctx, job, steps, nvtx=None):
     return e0.elapsed_time(e1)
 
 
-# DRAM bytes per Z-plane of the adjoint NFFT's two kernels, from ncu captures of
-# 32-plane launches on the same geometry (profiles/spread_colifft_cfg2_32planes.md,
-# which lists both): dram__bytes_read.sum + dram__bytes_write.sum / 32.
-MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((75.449856e6 + 71.426048e6)      # k_spread_colifft
+# DRAM bytes per Z-plane of the adjoint NFFT's three kernels, from ncu captures
+# of 32-plane launches on the same geometry: dram__bytes_read.sum +
+# dram__bytes_write.sum / 32.
+MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((163.802880e6 + 218.726656e6)    # k_spread_gather
+                                      + (256.0e6 + 96.0e6)             # k_colifft (model)
                                       + (100.737792e6 + 36.037120e6)) / 32  # k_rowifft_crop
 
 
 def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):
-    """Roofline of the dominant kernel pair, the adjoint NFFT (k_spread_colifft +
-    k_rowifft_crop).  Its unit is one Z-plane's adjoint NFFT, whose algorithmic bytes
-    are those of the unfused NFFT: c (P^2 + 4 n^2 + M) -- coefficients, the n x n
-    oversampled grid written, transformed (read + write) and read back, and the node
-    values.  achieved = units x that / the two kernels' measured time."""
+    """Roofline of the dominant kernel group, the adjoint NFFT (k_spread_gather
+    + k_colifft + k_rowifft_crop).  Its unit is one Z-plane's adjoint NFFT,
+    whose algorithmic bytes are those of the unfused NFFT: c (P^2 + 4 n^2 + M)
+    -- coefficients, the n x n oversampled grid written, transformed (read +
+    write) and read back, and the node values.  achieved = units x that / the
+    kernels' measured time."""
     total = sum(v[0] for v in prof.values())
     shares = {k: round(v[0] / total, 4) for k, v in prof.items() if v[1] > 0}
     P, nz = r["np"], r["nz"]
@@ -223,51 +225,78 @@ def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):
     ms_s, n_s, _ = prof["spread"]
     ms_c, n_c, _ = prof["crop"]
     # 11 adjoint NFFTs of every Z-plane per outer iteration (CGNR: one before
-    # the loop, one per step)
+    # the loop, one per step); each runs the row pass once per chunk of planes
     units = 11 * nz * steps
-    planes_per_launch = units / max(1, n_s)
+    planes_per_launch = units / max(1, n_c)
     secs = (ms_s + ms_c) / 1e3
     achieved = units * unit / secs / 1e9
     return "adjoint NFFT", {
-        "bound": "hbm", "kernel": "adjoint NFFT (k_spread_colifft + k_rowifft_crop)",
+        "bound": "hbm",
+        "kernel": "adjoint NFFT (k_spread_gather + k_colifft + k_rowifft_crop)",
         "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
         "frac": round(achieved / peak_gbs, 4),
         "traffic": round(MEASURED_ADJOINT_TRAFFIC_PER_PLANE * planes_per_launch),
         "algorithmic_bytes_per_launch": unit * planes_per_launch,
         "algorithmic_bytes_per_unit": unit, "units_per_launch": planes_per_launch,
-        "avg_launch_ms": (ms_s + ms_c) / n_s, "peak_source": peak_kind}, shares
+        "avg_launch_ms": (ms_s + ms_c) / max(1, n_c), "peak_source": peak_kind}, shares
 
 
-def cpu_baseline_sample(proj, r, iters=1, threads=None):
-    """The oracle (CPU restatement, FP64) on a bounded sample of the same job:
-    `threads` Z-planes run the per-plane NFFT+CGNR work (one plane per host
-    thread), the volume phases (Z-FFTs, denoise, constraints) run on the
-    full volume; the plane phase is extrapolated linearly to nz planes."""
+def cpu_sample_inputs(r, nz):
+    """The tilt series of the workload's geometry with `nz` Z-planes (the
+    phantom cut to nz planes), simulated and noised by the oracle's own 2D1D
+    restatement on the host."""
+    import copy
+
+    from nudim_gb300.synth import CONFIGS, add_noise, blob_phantom
+    from oracle import orc
+    c = copy.deepcopy(CONFIGS[CFG])
+    c["phantom"]["shape"] = (nz,) + tuple(c["phantom"]["shape"][1:])
+    vol = blob_phantom(seed=20261203, **c["phantom"])
+    s = c["sim"]
+    return add_noise(orc.project_2d1d(vol, s["np"], s["gam_min"], s["gam_max"], s["interval"]),
+                     s["snr"], 20261204)
+
+
+def cpu_time_iterations(r, nz, threads, warmup, steps):
+    """The oracle (the CPU restatement, FP64) on the workload's geometry with
+    nz Z-planes: `warmup` untimed outer iterations, then `steps` timed ones,
+    every phase of each on the whole nz-plane volume (nothing extrapolated).
+    Returns (seconds per iteration, voxels per iteration)."""
     from oracle import orc
     orc.build()
-    threads = threads or os.cpu_count() or 1
-    kw = dict(nx=r["nx"], nz=r["nz"], np=r["np"], gam_min=r["gam_min"], gam_max=r["gam_max"],
-              interval=r["interval"], padangle=r["padangle"], nhio=r["nhio"], ner=r["ner"],
-              denoise=r["denoise"], weight=r["weight"], nthreads=threads,
-              plane_limit=min(threads, r["nz"]))
+    proj = cpu_sample_inputs(r, nz)
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    t0 = time.time()
+    kw = dict(nx=r["nx"], nz=nz, np=r["np"], gam_min=r["gam_min"], gam_max=r["gam_max"],
+              interval=r["interval"], padangle=r["padangle"], nhio=r["nhio"], ner=r["ner"],
+              denoise=r["denoise"], weight=r["weight"], nthreads=threads)
     R = orc.Recon(proj, **kw)
-    t_setup = time.time() - t0
-    R.iterate(iters)
-    tp, tv = R.times()
+    R.iterate(warmup)
+    t0 = time.perf_counter()
+    R.iterate(steps)
+    t = (time.perf_counter() - t0) / steps
     R.close()
-    nplanes = kw["plane_limit"]
-    t_iter = (tp * r["nz"] / nplanes + tv) / iters
-    V = r["nz"] * r["np"] ** 2
-    return {"value": V / t_iter, "unit": "voxel-iters/s", "cores": threads, "kind": "port",
-            "sample": "%d outer iteration(s) of the same job; per-plane NFFT+CGNR on %d of %d "
-                      "Z-planes (one per thread) extrapolated linearly, volume phases on the "
-                      "full volume; setup %.1f s untimed" % (iters, nplanes, r["nz"], t_setup),
-            "s_per_iter": t_iter}
+    return t, nz * r["np"] ** 2
 
 
-def serving_specs(n_jobs, seed, big_share=0.1, nhio=10, ner=10, weight=1):
+def cpu_baseline_sample(r, threads=None, steps=2):
+    """cpu_baseline: the oracle on the host cores, whole outer iterations of
+    the workload's geometry with one Z-plane per thread (all threads), and
+    with two Z-planes on one core (the single-thread figure)."""
+    threads = threads or os.cpu_count() or 1
+    nz = max(2, threads + (threads & 1))
+    t, vox = cpu_time_iterations(r, nz, threads, 1, steps)
+    t1, vox1 = cpu_time_iterations(r, 2, 1, 0, 1)
+    return {"value": vox / t, "unit": "voxel-iters/s", "cores": threads, "kind": "port",
+            "sample": "%d outer iterations (after 1 untimed) of the workload's geometry (np=nx=%d, "
+                      "61 tilts, the same options) with nz=%d Z-planes, one per thread, every phase "
+                      "on the whole volume, nothing extrapolated" % (steps, r["np"], nz),
+            "s_per_iter": t,
+            "single_core": {"value": vox1 / t1, "unit": "voxel-iters/s", "cores": 1,
+                            "sample": "1 outer iteration, nz=2 Z-planes, one thread",
+                            "s_per_iter": t1}}
+
+
+def serving_specs(n_jobs, seed, big_share=0.1, nhio=20, ner=30, weight=1):
     """Uneven jobs of the batched/serving configurations: nx from
     {96,128,160,192,256}, nz from 32..256 step 16, pad = round16(U(1.25,1.5)
     * nx), symmetric max tilt U{45..70}, step {1,2,3}; a `big_share` of the
@@ -365,12 +394,14 @@ def batched_bench(ctx, n_jobs, steps, warmup, precision, seed=20261206):
 
 
 def serving_bench(ctx, n_jobs, rate, precision, seed=20261205):
-    """Poisson arrivals at `rate` jobs/s into the continuous-batching server;
-    returns p50/p99 arrival-to-result latency and completed jobs/s."""
+    """Poisson arrivals at `rate` jobs/s into the continuous-batching server
+    of jobs of the serving configuration (the batched size mix plus 10 % of
+    384 x 384 x 192, each 20 HIO + 30 ER with TV); returns p50/p99
+    arrival-to-result latency and completed jobs/s."""
     import torch
 
     import nudim_gb300 as ng
-    inputs = uneven_inputs(ctx, serving_specs(n_jobs, seed))
+    inputs = uneven_inputs(ctx, serving_specs(n_jobs, seed, big_share=0.1, nhio=20, ner=30))
     arrivals = np.cumsum(np.random.default_rng(seed + 7).exponential(1.0 / rate, n_jobs))
     free, _ = torch.cuda.mem_get_info()
     srv = ng.Server(ctx, int(0.7 * free), max_active=16)
@@ -387,8 +418,83 @@ def serving_bench(ctx, n_jobs, rate, precision, seed=20261205):
     srv.close()
     log("serving: %d jobs, p50 %.3f s, p99 %.3f s" % (n_jobs, st.get("p50_s", -1), st.get("p99_s", -1)))
     st.update(arrival_rate_jobs_per_s=rate, jobs=n_jobs,
-              voxels_per_job_mean=float(np.mean([s["nz"] * s["np"] ** 2 for _, s in inputs])))
+              voxels_per_job_mean=float(np.mean([s["nz"] * s["np"] ** 2 for _, s in inputs])),
+              iterations_per_job="20 HIO + 30 ER, TV",
+              big_jobs=int(sum(1 for _, s in inputs if s["nx"] == 384)))
     return st
+
+
+def accuracy_leg(ctx, r, nz=16, snaps=(1, 2, 5, 10, 50, 75, 100)):
+    """Accuracy of the reduced-precision forms against the FP64 form on the
+    workload's geometry (384^2 planes, 61 tilts, the same options) with nz
+    Z-planes, over the whole 50 HIO + 50 ER: relative L2 of the volume after
+    each iteration in `snaps`, for the FP64 form on a tilt series perturbed by
+    1e-15, 1e-13 and 6e-8 (FP32's unit roundoff) relative -- the floors: how
+    far the FP64 loop itself moves under FP64- and FP32-sized input changes --
+    the mixed form, the mixed form with its HIO iterations in FP64
+    (correct_every = -1) and with an FP64 iteration every 10th
+    (correct_every = 10)."""
+    import copy
+
+    import nudim_gb300 as ng
+    from nudim_gb300.synth import CONFIGS, MASTER_SEED, make_inputs
+    c = copy.deepcopy(CONFIGS[CFG])
+    c["phantom"]["shape"] = (nz,) + tuple(c["phantom"]["shape"][1:])
+    rr = dict(r, nz=nz)
+    vol, proj = make_inputs(ctx, None, seed=MASTER_SEED, cfg=c)
+    total = rr["nhio"] + rr["ner"]
+    snaps = [s for s in snaps if s <= total]
+
+    def run(p, precision, correct=0):
+        kw = job_kwargs(rr, precision)
+        kw["correct_every"] = correct
+        job = ng.Job(ctx, **kw)
+        job.set_projections(p)
+        out, done = {}, 0
+        for sn in snaps:
+            job.step(sn - done)
+            done = sn
+            out[sn] = job.volume()
+        fp64_its = job.corrections() if precision == ng.MIXED else total
+        job.close()
+        return out, fp64_its
+
+    rl = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    t0 = time.perf_counter()
+    ref, _ = run(proj, ng.FP64)
+    def pert(eps):
+        return proj * (1.0 + eps * np.random.default_rng(1).standard_normal(proj.shape))
+    res = {"rel_l2_vs_fp64": {}, "fp64_iterations": {}}
+    for name, p, prec, corr in (("fp64_perturbed_1e-15", pert(1e-15), ng.FP64, 0),
+                                ("fp64_perturbed_1e-13", pert(1e-13), ng.FP64, 0),
+                                ("fp64_perturbed_6e-8", pert(6e-8), ng.FP64, 0),
+                                ("mixed", proj, ng.MIXED, 0),
+                                ("mixed_fp64_hio", proj, ng.MIXED, -1),
+                                ("mixed_correct_10", proj, ng.MIXED, 10)):
+        v, n64 = run(p, prec, corr)
+        res["rel_l2_vs_fp64"][name] = {str(k): rl(v[k], ref[k]) for k in snaps}
+        res["fp64_iterations"][name] = n64
+    res.update(config="workload geometry with nz=%d Z-planes: np=nx=%d, 61 tilts, %d HIO + %d ER, "
+                      "the workload's denoise and weighting" % (nz, rr["np"], rr["nhio"], rr["ner"]),
+               snapshots=snaps, seconds=time.perf_counter() - t0)
+    log("accuracy (nz=%d) after %d: floor(1e-13) %.2e, floor(6e-8) %.2e, mixed %.2e, "
+        "FP64 HIO %.2e" % (
+        nz, total, res["rel_l2_vs_fp64"]["fp64_perturbed_1e-13"][str(total)],
+        res["rel_l2_vs_fp64"]["fp64_perturbed_6e-8"][str(total)],
+        res["rel_l2_vs_fp64"]["mixed"][str(total)],
+        res["rel_l2_vs_fp64"]["mixed_fp64_hio"][str(total)]))
+    return res
+
+
+def fp64_peak():
+    """The FP64 and FP32 FMA rates of this GPU (bin/fp64_peak: independent FMA
+    chains, CUDA events), or None when the probe is missing."""
+    exe = os.path.join(ROOT, "nudim_gb300", "bin", "fp64_peak")
+    try:
+        out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+        return json.loads(out.stdout.strip().splitlines()[-1]) if out.returncode == 0 else None
+    except (OSError, ValueError, IndexError, subprocess.TimeoutExpired):
+        return None
 
 
 def large_bench(ctx, steps=10, warmup=3):
@@ -452,38 +558,20 @@ def large_bench(ctx, steps=10, warmup=3):
 
 # ------------------------------------------------------------------ arms
 def run_reference(args):
+    """The reference arm: the oracle (the CPU restatement of the reference's
+    loop, FP64) on all host cores.  A step is one whole outer iteration of the
+    workload's geometry with one Z-plane per host thread (every phase on the
+    whole volume, nothing extrapolated), so the run ends within minutes."""
     ws, rank, local = dist_env()
     dist = init_dist(ws, "gloo")
     if rank != 0:
         barrier(dist)
         return 0
-    import nudim_gb300 as ng
-    from nudim_gb300 import build as nb
-    from nudim_gb300.synth import add_noise, blob_phantom
-    from oracle import orc
     c, r = workload_config()
-    # the tilt series is simulated by the oracle's own 2D1D restatement
-    orc.build()
     threads = os.cpu_count() or 1
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    vol = blob_phantom(seed=20261203, **c["phantom"])
-    s = c["sim"]
-    proj = add_noise(orc.project_2d1d(vol, s["np"], s["gam_min"], s["gam_max"], s["interval"]),
-                     s["snr"], 20261204)
-    kw = dict(nx=r["nx"], nz=r["nz"], np=r["np"], gam_min=r["gam_min"], gam_max=r["gam_max"],
-              interval=r["interval"], padangle=r["padangle"], nhio=r["nhio"], ner=r["ner"],
-              denoise=r["denoise"], weight=r["weight"], nthreads=threads,
-              plane_limit=min(threads, r["nz"]))
-    R = orc.Recon(proj, **kw)
-    R.iterate(args.warmup)
-    tp0, tv0 = R.times()
-    R.iterate(args.steps)
-    tp1, tv1 = R.times()
-    R.close()
-    n = kw["plane_limit"]
-    t_iter = ((tp1 - tp0) * r["nz"] / n + (tv1 - tv0)) / args.steps
-    V = r["nz"] * r["np"] ** 2
-    value = V / t_iter
+    nz = r["nz"] if NZ_OVERRIDE else max(2, threads + (threads & 1))
+    t_iter, vox = cpu_time_iterations(r, nz, threads, args.warmup, args.steps)
+    value = vox / t_iter
     line = {
         "impl": "reference", "metric": "voxel-iters/s", "value": value, "unit": "voxel-iters/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_iter * 1e3,
@@ -491,9 +579,9 @@ def run_reference(args):
         "data": "synthetic", "config": config_block(r),
         "cpu_baseline": {"value": value, "unit": "voxel-iters/s", "cores": threads,
                          "kind": "port",
-                         "sample": "each step: 1 outer iteration, per-plane NFFT+CGNR on %d of "
-                                   "%d Z-planes (one per thread) extrapolated linearly, volume "
-                                   "phases on the full volume" % (n, r["nz"])},
+                         "sample": "each step: 1 whole outer iteration of the workload's geometry "
+                                   "(np=nx=%d, 61 tilts, the same options) with nz=%d Z-planes, one "
+                                   "per thread, every phase on the whole volume" % (r["np"], nz)},
         "e2e": {"value": value, "unit": "voxel-iters/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -590,24 +678,43 @@ def run_ours(args):
                "phases": phases}
         log("e2e: %.3e voxel-iters/s" % e2e["value"])
 
-    # ---- FP64 plain form on the same job (fewer steps: it is the slow form)
-    v64 = ms64 = err = err1 = None
+    # ---- FP64 plain form on the same job (fewer steps: it is the slow form),
+    # device resident and end to end through the C ABI
+    v64 = ms64 = err = err1 = e2e64 = None
     fp64_steps = max(1, args.fp64_steps)
     if not args.no_fp64:
+        t0 = time.perf_counter()
         job = ng.Job(ctx, **job_kwargs(r, ng.FP64))
         job.set_projections(proj)
+        job.sync()
+        t_setup64 = time.perf_counter() - t0
         job.step(1)
         vol64_1 = job.volume()
         job.step(args.warmup - 1)
         ctx.sync()
         vol64_w = job.volume()
         ms64 = timed_steps(ctx, job, fp64_steps)
+        t0 = time.perf_counter()
+        out64 = job.volume()
+        t_out64 = time.perf_counter() - t0
         job.close()
         ms64 = max_over_ranks(dist, ms64, dev)
         v64 = ws * V * fp64_steps / (ms64 / 1e3)
+        # end to end: the same phases as the mixed form's e2e (setup, the
+        # iterations, the volume to the host), the iterations timed above
+        t_e2e64 = max_over_ranks(dist, t_setup64 + ms64 / 1e3 + t_out64, dev)
+        e2e64 = {"value": ws * V * fp64_steps / t_e2e64, "unit": "voxel-iters/s",
+                 "h2d_bytes_per_step": int(proj.nbytes // fp64_steps),
+                 "d2h_bytes_per_step": int(out64.nbytes // fp64_steps),
+                 "phases": {"job_create_and_set_projections_s": t_setup64,
+                            "iterations_s": ms64 / 1e3, "volume_to_host_s": t_out64}}
         err = float(np.linalg.norm(vol_mixed_w - vol64_w) / np.linalg.norm(vol64_w))
         err1 = float(np.linalg.norm(vol_mixed_1 - vol64_1) / np.linalg.norm(vol64_1))
         log("fp64: %.2f ms/iteration, mixed vs fp64 rel L2 %.2e" % (ms64 / fp64_steps, err))
+    peak64 = fp64_peak() if not args.no_fp64 else None
+    acc = None
+    if not args.no_accuracy:
+        acc = accuracy_leg(ctx, r, nz=args.accuracy_nz)
 
     line = {
         "metric": "voxel-iters/s", "value": value, "unit": "voxel-iters/s", "n_gpus": ws,
@@ -622,11 +729,44 @@ def run_ours(args):
         "clocks": clk,
     }
     if v64 is not None:
+        P, nz = r["np"], r["nz"]
+        n = 2 * (1 << (P - 1).bit_length())
+        M = 181 * P
+        # FP64 flops of one outer iteration in the reference's parameters: per
+        # Z-plane 23 NFFTs, each 196 taps x 4 flops per node plus an n x n FFT
+        # (5 n^2 log2 n^2 flops)
+        flops = nz * 23 * (196 * 4 * M + 5 * n * n * np.log2(float(n * n)))
+        achieved = flops / (ms64 / fp64_steps / 1e3) / 1e12
         line["fp64_plain"] = {"value": v64, "unit": "voxel-iters/s",
-                              "ms_per_step": ms64 / fp64_steps, "steps": fp64_steps}
+                              "ms_per_step": ms64 / fp64_steps, "steps": fp64_steps,
+                              "e2e": e2e64,
+                              "roofline": {"bound": "fp64", "achieved": round(achieved, 4),
+                                           "peak": peak64["fp64_tflops"] if peak64 else None,
+                                           "unit": "TFLOP/s",
+                                           "frac": round(achieved / peak64["fp64_tflops"], 4)
+                                           if peak64 else None,
+                                           "flops_per_step": flops,
+                                           "peak_source": "measured FP64 FMA chains on this GPU "
+                                                          "(nudim_gb300/bin/fp64_peak)"},
+                              "fp64_peak_probe": peak64}
         line["mixed_over_fp64"] = value / v64
         line["rel_l2_mixed_vs_fp64_after_1_iteration"] = err1
         line["rel_l2_mixed_vs_fp64_after_warmup"] = err
+    if acc is not None:
+        tot = str(r["nhio"] + r["ner"])
+        rel_acc = acc["rel_l2_vs_fp64"]
+        line["accuracy"] = acc
+        line["rel_l2_mixed_vs_fp64_after_%s" % tot] = rel_acc["mixed"].get(tot)
+        line["rel_l2_fp64_floor_after_%s" % tot] = {
+            k: rel_acc["fp64_perturbed_" + k].get(tot) for k in ("1e-15", "1e-13", "6e-8")}
+        line["rel_l2_mixed_fp64_hio_vs_fp64_after_%s" % tot] = rel_acc["mixed_fp64_hio"].get(tot)
+        if v64 is not None:
+            # the FP64-HIO schedule's time per iteration from the two measured
+            # forms: nhio FP64 iterations, ner FP32 ones
+            t_sched = (r["nhio"] * ms64 / fp64_steps + r["ner"] * ms_max / args.steps) / (
+                r["nhio"] + r["ner"])
+            line["mixed_fp64_hio"] = {"ms_per_step": t_sched, "value": ws * V / (t_sched / 1e3),
+                                      "over_fp64": (ms64 / fp64_steps) / t_sched}
     if args.large:
         line["large"] = large_bench(ctx)
     if args.batch_jobs > 0:
@@ -638,7 +778,7 @@ def run_ours(args):
             line["serving"]["fp64_plain"] = serving_bench(ctx, args.serve_jobs, args.serve_rate,
                                                           ng.FP64)
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline_sample(proj, r)
+        line["cpu_baseline"] = cpu_baseline_sample(r)
     ctx.close()
     if rank == 0:
         print(json.dumps(line))
@@ -690,7 +830,11 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the accuracy leg (reduced-nz 50 HIO + 50 ER in every form)")
+    ap.add_argument("--accuracy-nz", type=int, default=16,
+                    help="Z-planes of the accuracy leg's job (default 16)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form leg")

@@ -102,6 +102,10 @@ template <typename T> struct JobState {
     cudaStream_t st = nullptr;  // the job's stream: every allocation is ordered on it
     cufftHandle zplan = 0;      // Z-axis FFT plan with its work area in zws
     Workspace zws;
+    // NFFT scratch of this state alone: the state's captured graph holds its
+    // address, so no other state (a mixed job's FP64 corrective state) may
+    // regrow it
+    Workspace ws;
     int *it = nullptr;          // device copy of the outer-iteration index
     cudaGraphExec_t gexec = nullptr;  // replay of one outer iteration
     bool graph_tried = false;
@@ -128,6 +132,7 @@ template <typename T> struct JobState {
         if (zplan) cufftDestroy(zplan);
         zplan = 0;
         ws_release(&zws);
+        ws_release(&ws);
         live = false;
     }
 };
@@ -156,6 +161,16 @@ struct nudim_job {
     // the device in the job's precision; sent to the host only on request
     void *vol0 = nullptr;
     int corrections = 0;  // corrective FP64 iterations run
+    // periodic FP64 residual check (correct_every with NUDIM_CORRECT_TOL > 0):
+    // R of the current volume in FP64 and FP32 land in check_host (pinned) and
+    // check_ev marks their arrival; the iteration it decides waits until then
+    bool check_pending = false;
+    cudaEvent_t check_ev = nullptr;
+    double *check_host = nullptr;
+    // a mixed job whose last iteration ran in FP64: the FP64 state's volume is
+    // the current one (the FP32 copy is refreshed before an FP32 iteration),
+    // so consecutive FP64 iterations never round the volume to FP32
+    bool fp64_owns = false;
 };
 
 struct nudim_nfft_plan {
@@ -208,7 +223,8 @@ template <typename T> static int state_init(nudim_job *jb, JobState<T> &s)
     int nz = jb->d.nz, np = jb->d.np, M = jb->M;
     size_t P2 = (size_t)np * np, V = P2 * nz;
     s.st = jb->stream;
-    NUDIM_TRY(s.pl.init(jb->ctx, jb->tabs, jb->stream, &jb->ws));
+    s.ws.st = jb->stream;
+    NUDIM_TRY(s.pl.init(jb->ctx, jb->tabs, jb->stream, &s.ws));
     s.bytes += s.pl.bytes;
     NUDIM_TRY(s.alloc(&s.img_a, V));
     NUDIM_TRY(s.alloc(&s.img_b, V));
@@ -402,6 +418,11 @@ template <typename T> static int state_iterate(nudim_job *jb, JobState<T> &s, in
         if (rc == NUDIM_OK && e == cudaSuccess && g &&
             cudaGraphInstantiate(&s.gexec, g, 0) != cudaSuccess)
             s.gexec = nullptr;
+        if (s.gexec) {
+            // the graph holds the scratch addresses: they must not move
+            s.ws.frozen = true;
+            s.zws.frozen = true;
+        }
         if (g) cudaGraphDestroy(g);
         cudaGetLastError();  // a failed capture leaves eager execution in place
     }
@@ -448,36 +469,113 @@ static double correct_tol()
     return v > 0 ? v : 0.0;
 }
 
-// The periodic FP64 residual check of a mixed job: R of the current volume in
-// both forms; *need = their relative difference exceeds tol.
-static int residual_check(nudim_job *jb, int nn, double tol, bool *need)
+// The periodic FP64 residual check of a mixed job, queued on the job's
+// stream: R of the current volume in both forms, copied to check_host, with
+// check_ev recorded after the copies.  Nothing here waits on the host.
+static int residual_issue(nudim_job *jb, int nn)
 {
     cudaStream_t st = jb->stream;
     size_t V = (size_t)jb->d.np * jb->d.np * jb->d.nz;
-    NUDIM_TRY(launch_to_double<float>(jb->s32.img_a, jb->s64.img_a, V, st));
+    if (jb->fp64_owns) NUDIM_TRY(launch_real_to<float>(jb->s64.img_a, jb->s32.img_a, V, st));
+    else NUDIM_TRY(launch_to_double<float>(jb->s32.img_a, jb->s64.img_a, V, st));
     NUDIM_TRY(state_residual<double>(jb, jb->s64, nn));
     NUDIM_TRY(state_residual<float>(jb, jb->s32, nn));
-    double r64 = 0, r32 = 0;
-    NUDIM_CUDA(cudaMemcpyAsync(&r64, jb->s64.rh + nn, sizeof(double), cudaMemcpyDeviceToHost, st));
-    NUDIM_CUDA(cudaMemcpyAsync(&r32, jb->s32.rh + nn, sizeof(double), cudaMemcpyDeviceToHost, st));
-    NUDIM_CUDA(cudaStreamSynchronize(st));
-    *need = !(fabs(r32 - r64) <= tol * fabs(r64));
+    NUDIM_CUDA(cudaMemcpyAsync(jb->check_host, jb->s64.rh + nn, sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+    NUDIM_CUDA(cudaMemcpyAsync(jb->check_host + 1, jb->s32.rh + nn, sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+    NUDIM_CUDA(cudaEventRecord(jb->check_ev, st));
     return NUDIM_OK;
 }
 
 // FP64 buffers of a mixed job take over from FP32 for one corrective
-// iteration: convert the volume, iterate in FP64, convert back.
+// iteration: the FP32 volume is widened (unless the previous iteration was
+// FP64 too), the iteration runs in FP64 and its R lands in the FP32 history.
 static int corrective_iteration(nudim_job *jb, int nn)
 {
     cudaStream_t st = jb->stream;
     size_t V = (size_t)jb->d.np * jb->d.np * jb->d.nz;
-    NUDIM_TRY(launch_to_double<float>(jb->s32.img_a, jb->s64.img_a, V, st));
+    if (!jb->fp64_owns) NUDIM_TRY(launch_to_double<float>(jb->s32.img_a, jb->s64.img_a, V, st));
     NUDIM_TRY(state_iterate<double>(jb, jb->s64, nn));
-    NUDIM_TRY(launch_real_to<float>(jb->s64.img_a, jb->s32.img_a, V, st));
+    jb->fp64_owns = true;
     // keep the FP32 R history complete
     NUDIM_CUDA(cudaMemcpyAsync(jb->s32.rh + nn, jb->s64.rh + nn, sizeof(double),
                                cudaMemcpyDeviceToDevice, st));
     return NUDIM_OK;
+}
+
+// An FP32 iteration of a mixed job, from the FP64 volume when the previous
+// iteration was FP64.
+static int mixed_iteration(nudim_job *jb, int nn)
+{
+    if (jb->fp64_owns) {
+        size_t V = (size_t)jb->d.np * jb->d.np * jb->d.nz;
+        NUDIM_TRY(launch_real_to<float>(jb->s64.img_a, jb->s32.img_a, V, jb->stream));
+        jb->fp64_owns = false;
+    }
+    return state_iterate<float>(jb, jb->s32, nn);
+}
+
+// Which iterations of a mixed job run in FP64: correct_every = k > 0, every
+// k-th (subject to the residual check); k < 0, every HIO iteration (nn < nhio).
+static bool fp64_iteration(const nudim_job *jb, int nn)
+{
+    const int k = jb->d.correct_every;
+    return k > 0 ? (nn + 1) % k == 0 : k < 0 ? nn < jb->d.nhio : false;
+}
+
+// Queue outer iteration jb->done of a job that has one left.  A mixed job's
+// check iteration (every correct_every-th, with NUDIM_CORRECT_TOL > 0) first
+// queues the residual check; the iteration itself is queued once its result
+// is on the host: with block, after waiting for it; without, only if it has
+// arrived (*issued = false otherwise, and a later call decides).
+static int job_advance(nudim_job *jb, bool block, bool *issued)
+{
+    *issued = false;
+    if (jb->done >= jb->d.nhio + jb->d.ner) return NUDIM_OK;
+    const int nn = jb->done;
+    if (jb->d.precision == NUDIM_FP64) {
+        NUDIM_TRY(state_iterate<double>(jb, jb->s64, nn));
+    } else if (fp64_iteration(jb, nn)) {
+        const double tol = jb->d.correct_every > 0 ? correct_tol() : 0.0;
+        bool need = true;
+        if (tol > 0) {
+            if (!jb->check_pending) {
+                NUDIM_TRY(residual_issue(jb, nn));
+                jb->check_pending = true;
+            }
+            cudaError_t q = block ? cudaEventSynchronize(jb->check_ev) : cudaEventQuery(jb->check_ev);
+            if (q == cudaErrorNotReady) return NUDIM_OK;
+            if (q != cudaSuccess) return cuda_fail(q, "residual check", __FILE__, __LINE__);
+            jb->check_pending = false;
+            const double r64 = jb->check_host[0], r32 = jb->check_host[1];
+            need = !(fabs(r32 - r64) <= tol * fabs(r64));
+        }
+        if (need) {
+            NUDIM_TRY(corrective_iteration(jb, nn));
+            jb->corrections++;
+        } else {
+            NUDIM_TRY(mixed_iteration(jb, nn));
+        }
+    } else {
+        NUDIM_TRY(mixed_iteration(jb, nn));
+    }
+    jb->done++;
+    *issued = true;
+    return NUDIM_OK;
+}
+
+// The serving loop's step: queue the job's next iteration unless it waits on
+// a residual check whose result has not arrived (never blocks the host).
+int job_try_step(nudim_job *jb, bool *issued)
+{
+    *issued = false;
+    if (!jb || !jb->ready) {
+        set_error("job_try_step: job not ready");
+        return NUDIM_ESTATE;
+    }
+    NUDIM_CUDA(cudaSetDevice(jb->ctx->device));
+    return job_advance(jb, false, issued);
 }
 
 static int validate(const nudim_job_desc *d)
@@ -527,12 +625,13 @@ static int validate(const nudim_job_desc *d)
     return NUDIM_OK;
 }
 
-// scratch of one fused NFFT pass (row spectra + partials of a chunk of planes):
-// NUDIM_FUSED_BUDGET_MB, default 1.5 GB (all Z-planes of most jobs in one pass)
+// scratch of one fused NFFT pass (a chunk of planes: row spectra + partials
+// in the trafo, column spectra + the oversampled grid in the adjoint):
+// NUDIM_FUSED_BUDGET_MB, default 3 GB (all Z-planes of most jobs in one pass)
 static size_t fused_budget_default()
 {
     const char *fb = getenv("NUDIM_FUSED_BUDGET_MB");
-    return fb ? (size_t)atol(fb) << 20 : ((size_t)1536 << 20);
+    return fb ? (size_t)atol(fb) << 20 : ((size_t)3072 << 20);
 }
 
 static size_t job_bytes(const nudim_job_desc *d, int A, bool both, size_t fused_budget)
@@ -548,8 +647,9 @@ static size_t job_bytes(const nudim_job_desc *d, int A, bool both, size_t fused_
         // node (4-column blocks): id + 12 weights, and 3 ints + 20 weights
         b += M * (11 * (4 + 12 * sT) + 5 * (12 + 20 * sT));
         b += nz * (size_t)cgnr_part_stride((int)M, (int)P2) * 8;
-        // fused-path workspace: row spectra + partials of one chunk of planes
-        size_t plane = (np * n1 + 5 * M) * sC, chunk = fused_budget / plane;
+        // fused-path workspace: row spectra + partials (trafo) or column
+        // spectra + grid (adjoint) of one chunk of planes
+        size_t plane = (np * n1 + std::max(5 * M, n1 * n1)) * sC, chunk = fused_budget / plane;
         b += (chunk < 1 ? 1 : chunk < nz ? chunk : nz) * plane;
         return b;
     };
@@ -672,7 +772,7 @@ int nudim_job_footprint(const nudim_job_desc *d, size_t *bytes)
 {
     NUDIM_TRY(validate(d));
     int A = polar_lines(d->gam_min, d->interval, d->padangle, nullptr, nullptr);
-    *bytes = job_bytes(d, A, d->precision == NUDIM_MIXED && d->correct_every > 0,
+    *bytes = job_bytes(d, A, d->precision == NUDIM_MIXED && d->correct_every != 0,
                        fused_budget_default());
     return NUDIM_OK;
 }
@@ -701,6 +801,8 @@ int nudim_job_create(nudim_ctx *ctx, const nudim_job_desc *desc, nudim_job **out
             ws_release(&j->ws);
             cudaStreamSynchronize(j->stream);
             cudaStreamDestroy(j->stream);
+            if (j->check_ev) cudaEventDestroy(j->check_ev);
+            if (j->check_host) cudaFreeHost(j->check_host);
         }
     } guard{jb.get()};
     jb->d = *desc;
@@ -732,7 +834,11 @@ int nudim_job_create(nudim_ctx *ctx, const nudim_job_desc *desc, nudim_job **out
         NUDIM_TRY(state_init<double>(jb.get(), jb->s64));
     } else {
         NUDIM_TRY(state_init<float>(jb.get(), jb->s32));
-        if (d.correct_every > 0) NUDIM_TRY(state_init<double>(jb.get(), jb->s64));
+        if (d.correct_every != 0) {
+            NUDIM_TRY(state_init<double>(jb.get(), jb->s64));
+            NUDIM_CUDA(cudaMallocHost(&jb->check_host, 2 * sizeof(double)));
+            NUDIM_CUDA(cudaEventCreateWithFlags(&jb->check_ev, cudaEventDisableTiming));
+        }
     }
     guard.j = nullptr;
     *out = jb.release();
@@ -749,6 +855,8 @@ int nudim_job_destroy(nudim_job *jb)
     if (jb->vol0) cudaFreeAsync(jb->vol0, jb->stream);
     cudaStreamSynchronize(jb->stream);
     cudaStreamDestroy(jb->stream);
+    if (jb->check_ev) cudaEventDestroy(jb->check_ev);
+    if (jb->check_host) cudaFreeHost(jb->check_host);
     delete jb;
     return NUDIM_OK;
 }
@@ -803,6 +911,7 @@ int nudim_job_set_projections(nudim_job *jb, const double *proj, size_t n)
     auto cleanup = [&]() {
         for (void *q : tmp) cudaFreeAsync(q, st);
         p1.release();
+        ws_release(&jb->ws);  // the tilt-series NFFT's scratch
         cudaStreamSynchronize(st);
     };
     double *d_proj = nullptr;
@@ -849,12 +958,17 @@ int nudim_job_set_projections(nudim_job *jb, const double *proj, size_t n)
     }
     // ---- reorder/mask/fill + initial inverse NFFT
     if (!rc) {
+        jb->fp64_owns = false;
         if (d.precision == NUDIM_FP64)
             rc = state_setup<double>(jb, jb->s64, d_tomo, d_order, d_rank, d_fill);
         else {
-            rc = state_setup<float>(jb, jb->s32, d_tomo, d_order, d_rank, d_fill);
+            // a job whose HIO iterations run in FP64 starts from the FP64
+            // initial inverse, so those iterations are the FP64 form's own
+            const bool hio64 = d.correct_every < 0 && d.nhio > 0;
+            rc = state_setup<float>(jb, jb->s32, d_tomo, d_order, d_rank, d_fill, !hio64);
             if (!rc && jb->s64.live)
-                rc = state_setup<double>(jb, jb->s64, d_tomo, d_order, d_rank, d_fill, false);
+                rc = state_setup<double>(jb, jb->s64, d_tomo, d_order, d_rank, d_fill, hio64);
+            jb->fp64_owns = hio64;
         }
     }
     if (!rc) {
@@ -868,8 +982,10 @@ int nudim_job_set_projections(nudim_job *jb, const double *proj, size_t n)
             set_error("out of device memory for the initial volume");
             rc = NUDIM_ENOMEM;
         }
-        if (!rc && cudaMemcpyAsync(jb->vol0, src, bytes, cudaMemcpyDeviceToDevice, st) !=
-                       cudaSuccess) {
+        if (!rc && jb->fp64_owns) {
+            rc = launch_real_to<float>(jb->s64.img_a, (float *)jb->vol0, V, st);
+        } else if (!rc && cudaMemcpyAsync(jb->vol0, src, bytes, cudaMemcpyDeviceToDevice, st) !=
+                              cudaSuccess) {
             set_error("initial volume copy failed");
             rc = NUDIM_ECUDA;
         }
@@ -891,37 +1007,40 @@ int nudim_step(nudim_ctx *ctx, nudim_job *const *jobs, int njobs, int iters)
         return NUDIM_EINVAL;
     }
     NUDIM_CUDA(cudaSetDevice(ctx->device));
-    for (int it = 0; it < iters; it++) {
-        for (int k = 0; k < njobs; k++) {
-            nudim_job *jb = jobs[k];
-            if (!jb || jb->ctx != ctx) {
-                set_error("job %d does not belong to this context", k);
-                return NUDIM_EINVAL;
-            }
-            if (!jb->ready) {
-                set_error("nudim_step before nudim_job_set_projections");
-                return NUDIM_ESTATE;
-            }
-            int total = jb->d.nhio + jb->d.ner;
-            if (jb->done >= total) continue;
-            int nn = jb->done;
-            if (jb->d.precision == NUDIM_FP64) {
-                NUDIM_TRY(state_iterate<double>(jb, jb->s64, nn));
-            } else if (jb->d.correct_every > 0 && (nn + 1) % jb->d.correct_every == 0) {
-                const double tol = correct_tol();
-                bool need = true;
-                if (tol > 0) NUDIM_TRY(residual_check(jb, nn, tol, &need));
-                if (need) {
-                    NUDIM_TRY(corrective_iteration(jb, nn));
-                    jb->corrections++;
-                } else {
-                    NUDIM_TRY(state_iterate<float>(jb, jb->s32, nn));
-                }
-            } else {
-                NUDIM_TRY(state_iterate<float>(jb, jb->s32, nn));
-            }
-            jb->done++;
+    std::vector<int> target(njobs);
+    for (int k = 0; k < njobs; k++) {
+        nudim_job *jb = jobs[k];
+        if (!jb || jb->ctx != ctx) {
+            set_error("job %d does not belong to this context", k);
+            return NUDIM_EINVAL;
         }
+        if (!jb->ready) {
+            set_error("nudim_step before nudim_job_set_projections");
+            return NUDIM_ESTATE;
+        }
+        target[k] = std::min(jb->done + iters, jb->d.nhio + jb->d.ner);
+    }
+    // Round-robin: one iteration of each job per round.  A job whose next
+    // iteration waits on its residual check's result is passed over until
+    // the result is in; the host blocks only when every remaining iteration
+    // waits on one.
+    for (;;) {
+        bool left = false, progress = false;
+        for (int k = 0; k < njobs; k++) {
+            if (jobs[k]->done >= target[k]) continue;
+            left = true;
+            bool issued = false;
+            NUDIM_TRY(job_advance(jobs[k], false, &issued));
+            progress = progress || issued;
+        }
+        if (!left) break;
+        if (!progress)
+            for (int k = 0; k < njobs; k++)
+                if (jobs[k]->done < target[k]) {
+                    bool issued = false;
+                    NUDIM_TRY(job_advance(jobs[k], true, &issued));
+                    break;
+                }
     }
     return NUDIM_OK;
 }
@@ -940,7 +1059,7 @@ int nudim_job_get_volume(nudim_job *jb, double *out, size_t n, int crop)
     cudaStream_t st = jb->stream;
     std::vector<double> full;
     double *dst = crop ? (full.resize(V), full.data()) : out;
-    if (d.precision == NUDIM_FP64) {
+    if (d.precision == NUDIM_FP64 || jb->fp64_owns) {
         NUDIM_CUDA(cudaMemcpyAsync(dst, jb->s64.img_a, sizeof(double) * V, cudaMemcpyDeviceToHost, st));
     } else {
         double *tmpd = (double *)jb->s32.z;  // V complex floats = V doubles of room

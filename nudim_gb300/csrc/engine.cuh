@@ -53,7 +53,7 @@ struct nudim_ctx {
     void *ws = nullptr;          // shared oversampled-grid workspace
     size_t ws_bytes = 0;
     size_t grid_budget = 0;      // bytes a single NFFT pass may use for grids
-    size_t fused_budget = 0;     // bytes of row spectra + partials per fused pass (L2 sized)
+    size_t fused_budget = 0;     // scratch bytes of one fused NFFT pass over a chunk of planes
     bool use_fused = true;       // NFFT path: fused (default) or cuFFT grid path
     // NUDIM_CTX_AUTOTUNE: the fused plan choice (trafo column width, planes per
     // spreading CTA) found fastest for each (N0, N1, M, element size)
@@ -69,10 +69,14 @@ namespace nudim {
 
 // Stream-ordered scratch owned by one stream (a job or the context): grows
 // with cudaFreeAsync/cudaMallocAsync on that stream, never syncs the device.
+// Once a CUDA graph has captured launches that use it, the workspace is
+// frozen: a later request for more bytes is an error (NUDIM_ESTATE) instead
+// of a reallocation that would leave the graph holding a freed address.
 struct Workspace {
     void *p = nullptr;
     size_t bytes = 0;
     cudaStream_t st = nullptr;
+    bool frozen = false;
 };
 int ws_get(Workspace *w, size_t bytes, void **out);
 void ws_release(Workspace *w);
@@ -164,11 +168,12 @@ template <typename T> struct NfftDev {
     // fused path (nfft_fused.cu): no oversampled grid in HBM
     bool fused = false;
     int BC = 0, nblk = 0, smax = 0, rows = 4;    // trafo column blocks
-    int BCa = 0, nblka = 0, nbands = 0, Pa = 1;  // adjoint column blocks, planes per CTA
+    int BCa = 0, nblka = 0, nbands = 0, ntiles = 0;  // adjoint column blocks and tiles
+    int Pa = 1;                                     // planes per spreading-gather pass
     // caps on the trafo column width and the planes per spreading CTA for
     // init_fused (0: the defaults, or the NUDIM_TUNE_* environment knobs)
     int tune_bc = 0, tune_planes = 0;
-    size_t smem_col = 0, smem_row = 0, smem_spread = 0;
+    size_t smem_col = 0, smem_row = 0, smem_spread = 0, smem_colifft = 0;
     C *tw0 = nullptr, *tw1 = nullptr;
     int *blk_off = nullptr, *ent = nullptr, *band_off = nullptr, *band_node = nullptr,
         *band_ord = nullptr;
@@ -195,7 +200,7 @@ template <typename T> struct NfftDev {
     int init_fused(const NfftTables &t, cudaStream_t st);
     int autotune(const NfftTables &t, cudaStream_t st);
     void release_fused();
-    int fused_chunk(int nplanes) const;
+    int fused_chunk(int nplanes, size_t per_plane) const;
     int trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia, cudaStream_t st);
     int adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca,
                       cudaStream_t st);
@@ -219,6 +224,11 @@ int cgnr_run(NfftDev<T> &pl, int nplanes, const cplx_t<T> *y, const T *w, cplx_t
              const T *f_real, bool f_zero, int iters, CgnrBuffers<T> &b, cudaStream_t st);
 
 int cgnr_part_stride(int M, int N);
+
+// The serving loop's step (api.cu): queue the job's next outer iteration
+// unless it waits on a residual check whose result has not reached the host
+// (*issued = false then); never blocks the host.
+int job_try_step(nudim_job *jb, bool *issued);
 
 // ------------------------------------------------------------ volume ops
 template <typename T>

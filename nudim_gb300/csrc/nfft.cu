@@ -229,6 +229,11 @@ template <typename T> int NfftDev<T>::workspace(size_t nb, void **p)
 
 int ws_get(Workspace *w, size_t bytes, void **out)
 {
+    if (bytes > w->bytes && w->frozen) {
+        set_error("workspace of %zu bytes asked for %zu after a graph captured it", w->bytes,
+                  bytes);
+        return NUDIM_ESTATE;
+    }
     if (bytes > w->bytes) {
         if (w->p) NUDIM_CUDA(cudaFreeAsync(w->p, w->st));
         w->p = nullptr;
@@ -245,6 +250,7 @@ void ws_release(Workspace *w)
     if (w->p) cudaFreeAsync(w->p, w->st);
     w->p = nullptr;
     w->bytes = 0;
+    w->frozen = false;
 }
 
 template <typename T> void NfftDev<T>::release()

@@ -405,238 +405,196 @@ k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ 
     }
 }
 
-// ================================================================ K4 spread + column IFFT
-// Gather form over P planes at once: warp w takes tiles of R = 32/BC rows x
-// BC columns of the block (one grid point per lane), longest list first,
-// from a shared counter, and sums for its point and each of the P planes
-// the contributions of the tile's node list in ascending node order -- the
-// per-point order of the grid path.  Each list entry carries the tile's
-// window weights (R row weights, BC column weights, zero outside the
-// window), so a node costs a lane two weight reads, one product and two
-// FMAs per plane.  FP32: plain sums within a batch of NB nodes, compensated
-// (Neumaier) sums across batches.  The tile sums go to S_p; then per plane
-// n0-point inverse FFTs of the BC columns.
-//
-// A warp walks its batches (NB list entries; an empty tile is one empty
-// batch) as a two-stage pipeline: while batch i is summed, the weights and
-// node ids of batch i+1 -- the next batch of the tile or the first of the
-// warp's next tile -- arrive by cp.async in the other stage buffer.
-// Shared memory: S_0..S_{P-1}, K (BC x n0 complex each; K is FFT scratch),
-// then the warps' stages.
-constexpr int kSpreadWarps = 16;
-constexpr int kMaxBands = 1024;
+// ================================================================ K4a spreading gather
+// The adjoint's spreading as a gather into the oversampled grid G of a chunk
+// of planes.  The grid is cut into tiles of R = 32 / BC rows x BC columns
+// (one grid point per warp lane); each tile has the ascending list of the
+// nodes whose window meets it, every entry carrying the tile's R row and BC
+// column window weights (zero outside the window).  A warp takes one tile
+// for P planes at a time and walks its list in chunks of 32 entries: lane l
+// stages entry l's weights and its node's P (weighted) values in the warp's
+// shared-memory stage, then every lane sums, for its grid point and each
+// plane, q0(row) q1(col) f over the chunk -- one paired FMA per plane and
+// entry in FP32.  FP32: plain sums within a chunk, Neumaier-compensated
+// across chunks; FP64: fused multiply-adds in ascending node order.  The tile's 32 points of each plane are one
+// contiguous 256-byte (FP32) store: G is laid out column block by column
+// block, [plane][block][row][column in block], which is also the order the
+// column IFFT reads.  Tiles come in one global order, longest list first;
+// a CTA takes kGatherTilesPerCta consecutive tiles of it and its warps
+// share them out through a shared counter.  No grid point has two writers
+// and every sum has a fixed order: the results are deterministic.
+constexpr int kGatherWarps = 8;
+constexpr int kGatherTilesPerCta = 32;
 
-template <typename T> __host__ __device__ constexpr int spread_batch() { return sizeof(T) == 4 ? 16 : 8; }
-
-// stage of one warp: node values [P][NB], weights [2][NB][W], node ids [2][NB]
-template <typename T, int P> __host__ __device__ constexpr size_t spread_stage_bytes(int W)
+// node values of a stage: row stride in complex elements (padded so the
+// lanes' 16-byte staging stores meet distinct banks)
+template <int P> __host__ __device__ constexpr int gather_fs_stride() { return P == 1 ? 1 : P + 2; }
+template <typename T, int P> __host__ __device__ constexpr size_t gather_stage_bytes(int W)
 {
-    return (size_t)spread_batch<T>() * (P * sizeof(cplx_t<T>) + 2 * W * sizeof(T) + 2 * sizeof(int));
-}
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes)
-{
-    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem),
-                 "r"(src_bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem, int src_bytes)
-{
-    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem),
-                 "r"(src_bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait()
-{
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+    return 32 * ((size_t)W * sizeof(T) + (size_t)gather_fs_stride<P>() * sizeof(cplx_t<T>));
 }
 
 template <typename T, bool WEIGHTED, int P>
-__global__ void __launch_bounds__(32 * kSpreadWarps, 1)
-k_spread_colifft(SpreadArgs<T> sa, const int *__restrict__ band_off,
-                 const int *__restrict__ band_ord, const int *__restrict__ band_node,
-                 const T *__restrict__ band_w, int nbands, int N0, int n0, int logn0, int n1,
-                 int BC, int nb_planes, const cplx_t<T> *__restrict__ tw0, int plane0,
-                 cplx_t<T> *__restrict__ Hp)
+__global__ void __launch_bounds__(32 * kGatherWarps)
+k_spread_gather(SpreadArgs<T> sa, const int *__restrict__ tile_ord, int ntiles,
+                const int *__restrict__ band_off, const int *__restrict__ band_node,
+                const T *__restrict__ band_w, int nbands, int n0, int n1, int BC,
+                int nb_planes, int plane0, cplx_t<T> *__restrict__ G)
 {
     using C = cplx_t<T>;
-    constexpr int NB = spread_batch<T>();
-    constexpr int TV = 16 / sizeof(T);  // weights per 16-byte copy
+    constexpr int FS = gather_fs_stride<P>();
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ int next_tile, s_off[kMaxBands + 1], s_ord[kMaxBands];
-    const size_t buf = fft_buf((size_t)BC * n0);  // S_p and K, each with the FFT's padding
-    C *S = (C *)smraw, *K = S + P * buf;
-    const int cb = blockIdx.x, pb = blockIdx.y * P;
-    const int np = min(P, nb_planes - pb);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    const int R = 32 / BC, W = R + BC;
-    unsigned char *wst = (unsigned char *)(K + buf) + warp * spread_stage_bytes<T, P>(W);
-    C *fs = (C *)wst;                        // [NB][P]
-    T *ws = (T *)(fs + P * NB);              // [2][NB * W]
-    int *jb = (int *)(ws + 2 * NB * W);      // [2][NB]
-    const int rr = lane / BC, cc = lane - rr * BC;
-    for (int i = threadIdx.x; i <= nbands; i += blockDim.x) {
-        s_off[i] = band_off[(size_t)cb * nbands + i];
-        if (i < nbands) s_ord[i] = band_ord[(size_t)cb * nbands + i];
-    }
-    if (threadIdx.x == 0) next_tile = nwarps;
+    __shared__ int next_tile;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int R = 32 / BC, W = R + BC, nblk = n1 / BC;
+    T *ws = (T *)(smraw + warp * gather_stage_bytes<T, P>(W));  // [32][W] weights
+    C *fs = (C *)(ws + 32 * W);                                 // [32][FS] node values
+    const int pb = blockIdx.y * P, np = min(P, nb_planes - pb);
+    const int t0 = blockIdx.x * kGatherTilesPerCta;
+    const int t1 = min(ntiles, t0 + kGatherTilesPerCta);
+    if (threadIdx.x == 0) next_tile = t0 + kGatherWarps;
     __syncthreads();
-    auto fetch = [&]() {
-        int nv = 0;
-        if (lane == 0) nv = atomicAdd(&next_tile, 1);
-        return __shfl_sync(0xffffffffu, nv, 0);
-    };
-    // copy batch [base, min(base + NB, end)) of the lists into stage s
-    auto issue = [&](int s, int base, int end) {
-        const int n = min(NB, end - base);
-        T *wd = ws + s * NB * W;
-        const T *wsrc = band_w + (size_t)base * W;
-        for (int q = lane; q < NB * W / TV; q += 32) {
-            bool in = q * TV < n * W;
-            cp_async16(wd + q * TV, in ? (const void *)(wsrc + q * TV) : (const void *)band_w,
-                       in ? 16 : 0);
-        }
-        if (lane < NB) {
-            bool in = lane < n;
-            cp_async4(jb + s * NB + lane, in ? (const void *)(band_node + base + lane)
-                                             : (const void *)band_node,
-                      in ? 4 : 0);
-        }
-    };
-    int it = warp, v = 0, base = 0, end = 0;
-    if (it < nbands) {
-        v = s_ord[it];
-        base = s_off[v];
-        end = s_off[v + 1];
-        issue(0, base, end);
-    }
-    cp_async_commit();
-    int it_nx = fetch();
-    int sb = 0;
-    T ar[P], ai[P];
-    Comp<T> kr[P], ki[P];
+    const int rr = lane / BC, cc = lane - rr * BC;
+    const int wv16 = W * (int)sizeof(T) / 16;  // 16-byte vectors of an entry's weights
+    int it = t0 + warp;
+    while (it < t1) {
+        const int tile = tile_ord[it];
+        const int beg = band_off[tile], end = band_off[tile + 1];
+        T ar[P], ai[P];
+        Comp<T> kr[P], ki[P];
 #pragma unroll
-    for (int p = 0; p < P; p++) {
-        ar[p] = ai[p] = T(0);
-        kr[p].init();
-        ki[p].init();
-    }
-    while (it < nbands) {
-        // the batch after this one
-        const bool last = base + NB >= end;
-        int nit = it, nv = v, nbase = base + NB, nend = end;
-        if (last) {
-            nit = it_nx;
-            if (nit < nbands) {
-                nv = s_ord[nit];
-                nbase = s_off[nv];
-                nend = s_off[nv + 1];
-            }
+        for (int p = 0; p < P; p++) {
+            ar[p] = ai[p] = T(0);
+            kr[p].init();
+            ki[p].init();
         }
-        if (nit < nbands) issue(sb ^ 1, nbase, nend);
-        cp_async_commit();
-        cp_async_wait<1>();
-        __syncwarp();
-        const int n = min(NB, end - base);
-        // node values of this batch (zero past the list end)
-        if (lane < NB) {
-            int jl = jb[sb * NB + lane];
-            T wv = (WEIGHTED && lane < n) ? sa.w[jl] : T(1);
+        for (int base = beg; base < end; base += 32) {
+            const int n = min(32, end - base);
+            if (lane < n) {
+                const int e = base + lane;
+                const int j = band_node[e];
+                const float4 *src = reinterpret_cast<const float4 *>(band_w + (size_t)e * W);
+                float4 *dst = reinterpret_cast<float4 *>(ws + lane * W);
+                for (int q = 0; q < wv16; q++) dst[q] = src[q];
+                const T wv = WEIGHTED ? sa.w[j] : T(1);
 #pragma unroll
-            for (int p = 0; p < P; p++) {
-                C fv = mkc<T>(0, 0);
-                if (lane < n && p < np) {
-                    fv = sa.f[(size_t)(plane0 + pb + p) * sa.f_stride + jl];
-                    if (WEIGHTED) fv = mkc<T>(wv * fv.x, wv * fv.y);
+                for (int p = 0; p < P; p++) {
+                    C fv = mkc<T>(0, 0);
+                    if (p < np) {
+                        fv = sa.f[(size_t)(plane0 + pb + p) * sa.f_stride + j];
+                        if (WEIGHTED) fv = mkc<T>(wv * fv.x, wv * fv.y);
+                    }
+                    fs[lane * FS + p] = fv;
                 }
-                fs[lane * P + p] = fv;
             }
-        }
-        __syncwarp();
-        const T *wc = ws + sb * NB * W;
-        float2 bs[P];  // FP32 form: the batch sums (re, im) of each plane
+            __syncwarp();
+            if constexpr (sizeof(T) == 4) {
+                float2 bs[P];  // the chunk's sums (re, im) of each plane
 #pragma unroll
-        for (int p = 0; p < P; p++) bs[p] = make_float2(0.f, 0.f);
-        // nodes k0 .. k0 + K of the batch (weights past the list end are zero)
-        auto nodes = [&](auto kcount) {
-            constexpr int K = decltype(kcount)::value;
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                T q0 = wc[k * W + rr], q1 = wc[k * W + R + cc];
-                if constexpr (sizeof(T) == 4) {
-                    // one paired FMA per plane: (re, im) += q * f
-                    const float q = q0 * q1;
+                for (int p = 0; p < P; p++) bs[p] = make_float2(0.f, 0.f);
+#pragma unroll 2
+                for (int k = 0; k < n; k++) {
+                    const float q = ws[k * W + rr] * ws[k * W + R + cc];
                     const float2 qq = make_float2(q, q);
                     if constexpr (P % 2 == 0) {
 #pragma unroll
                         for (int p = 0; p < P; p += 2) {
-                            const float4 f2 = *reinterpret_cast<const float4 *>(fs + k * P + p);
+                            const float4 f2 = *reinterpret_cast<const float4 *>(fs + k * FS + p);
                             bs[p] = __ffma2_rn(qq, make_float2(f2.x, f2.y), bs[p]);
                             bs[p + 1] = __ffma2_rn(qq, make_float2(f2.z, f2.w), bs[p + 1]);
                         }
                     } else {
 #pragma unroll
                         for (int p = 0; p < P; p++) {
-                            const C fv = fs[k * P + p];
+                            const C fv = fs[k * FS + p];
                             bs[p] = __ffma2_rn(qq, make_float2(fv.x, fv.y), bs[p]);
                         }
                     }
-                } else {
+                }
+#pragma unroll
+                for (int p = 0; p < P; p++) {
+                    kr[p].add(bs[p].x);
+                    ki[p].add(bs[p].y);
+                }
+            } else {
+                // FP64: the point's weight once per entry, then one fused
+                // multiply-add per plane and component (the FP64 pipe is
+                // the bound on this GPU)
+                for (int k = 0; k < n; k++) {
+                    const T q = ws[k * W + rr] * ws[k * W + R + cc];
 #pragma unroll
                     for (int p = 0; p < P; p++) {
-                        C fv = fs[k * P + p];
-                        ar[p] += q1 * (q0 * fv.x);
-                        ai[p] += q1 * (q0 * fv.y);
+                        const C fv = fs[k * FS + p];
+                        ar[p] = fma(q, fv.x, ar[p]);
+                        ai[p] = fma(q, fv.y, ai[p]);
                     }
                 }
             }
-        };
-        // a short batch (the tail of most lists) runs the half-length loop
-        if (n <= NB / 2) nodes(std::integral_constant<int, NB / 2>());
-        else nodes(std::integral_constant<int, NB>());
-        if constexpr (sizeof(T) == 4) {
-#pragma unroll
-            for (int p = 0; p < P; p++) {
-                kr[p].add(bs[p].x);
-                ki[p].add(bs[p].y);
-            }
+            __syncwarp();  // the stage is refilled by the next chunk
         }
-        __syncwarp();  // stage sb and fs are refilled two steps on
-        if (last) {
-            const int r = v * R + rr;
+        const int b = tile / nbands, v = tile - b * nbands;
 #pragma unroll
-            for (int p = 0; p < P; p++) {
+        for (int p = 0; p < P; p++) {
+            if (p < np) {
                 if (sizeof(T) == 4) {
                     ar[p] = kr[p].value();
                     ai[p] = ki[p].value();
                 }
-                S[p * buf + (size_t)cc * n0 + r] = mkc<T>(ar[p], ai[p]);
-                ar[p] = ai[p] = T(0);
-                kr[p].init();
-                ki[p].init();
+                G[(((size_t)(pb + p) * nblk + b) * n0 + (size_t)v * R) * BC + lane] =
+                    mkc<T>(ar[p], ai[p]);
             }
-            if (nit < nbands) it_nx = fetch();
         }
-        it = nit;
-        v = nv;
-        base = nbase;
-        end = nend;
-        sb ^= 1;
+        int nt = 0;
+        if (lane == 0) nt = atomicAdd(&next_tile, 1);
+        it = __shfl_sync(0xffffffffu, nt, 0);
     }
-    cp_async_wait<0>();
-    __syncthreads();
-    for (int p = 0; p < np; p++) {
-        C *G = block_fft<T, +1>(S + p * buf, K, n0, logn0, BC, tw0);
-        C *Hb = Hp + (size_t)(pb + p) * N0 * n1 + cb * BC;
-        for (int idx = threadIdx.x; idx < N0 * BC; idx += blockDim.x) {
-            int a = idx / BC, cl = idx - a * BC;
-            int l0 = (a - N0 / 2) & (n0 - 1);
-            Hb[(size_t)a * n1 + cl] = G[(size_t)cl * n0 + l0];
+}
+
+// ================================================================ K4b column IFFT
+// One CTA per (column block, plane): the block's n0 x BC grid values (one
+// contiguous run of G) into shared memory column by column, BC inverse
+// n0-point FFTs, the N0 kept rows (a - N0/2 mod n0) written to H'.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_colifft(const cplx_t<T> *__restrict__ G, int N0, int n0, int logn0, int n1, int BC,
+          const cplx_t<T> *__restrict__ tw0, cplx_t<T> *__restrict__ Hp)
+{
+    using C = cplx_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *A = (C *)smraw, *B = A + fft_buf((size_t)BC * n0);
+    const int cb = blockIdx.x, b = blockIdx.y, nblk = n1 / BC;
+    const C *Gb = G + ((size_t)b * nblk + cb) * n0 * BC;
+    // row l0's BC values are contiguous: thread l0 moves them to the BC
+    // columns (consecutive threads, consecutive rows: no bank conflicts);
+    // four (FP32) or two (FP64) rows per thread in flight
+    {
+        constexpr int U = sizeof(T) == 4 ? 4 : 2;
+        for (int base = threadIdx.x; base < n0; base += U * blockDim.x) {
+            C v[U][4];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int l0 = base + u * blockDim.x;
+                if (l0 < n0)
+                    for (int c = 0; c < BC && c < 4; c++) v[u][c] = Gb[(size_t)l0 * BC + c];
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int l0 = base + u * blockDim.x;
+                if (l0 < n0)
+                    for (int c = 0; c < BC && c < 4; c++) A[(size_t)c * n0 + l0] = v[u][c];
+            }
         }
-        __syncthreads();
+        for (int c = 4; c < BC; c++)  // blocks wider than 4 columns
+            for (int l0 = threadIdx.x; l0 < n0; l0 += blockDim.x)
+                A[(size_t)c * n0 + l0] = Gb[(size_t)l0 * BC + c];
+    }
+    __syncthreads();
+    const C *R = block_fft<T, +1>(A, B, n0, logn0, BC, tw0);
+    C *Hb = Hp + (size_t)b * N0 * n1 + (size_t)cb * BC;
+    for (int idx = threadIdx.x; idx < N0 * BC; idx += blockDim.x) {
+        const int a = idx / BC, cl = idx - a * BC;
+        const int l0 = (a - N0 / 2) & (n0 - 1);
+        Hb[(size_t)a * n1 + cl] = R[(size_t)cl * n0 + l0];
     }
 }
 
@@ -742,36 +700,33 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     BCa = L.BCa;
     nblka = L.nblka;
     nbands = L.nbands;
-    if (nbands > kMaxBands) return NUDIM_EINVAL;
+    ntiles = nblka * nbands;
     // rows per CTA in the row passes: two (padded) rows x n1 complex buffers within 112 KB
     rows = 4;
     while (rows > 1 && 2 * sizeof(C) * fft_buf((size_t)rows * t.n1) > ((size_t)112 << 10)) rows--;
     smem_col = 2 * sizeof(C) * fft_buf((size_t)BC * n0);
     smem_row = 2 * sizeof(C) * fft_buf((size_t)rows * n1);
-    // adjoint column pass: as many planes per CTA (4, 2, 1) as fit in 212 KB
-    // of dynamic shared memory (8 KB of tile offsets and order are static)
-    const int Wa = 32 / BCa + BCa;
-    size_t bufa = sizeof(C) * fft_buf((size_t)BCa * n0);
-    auto spread_smem = [&](int p) -> size_t {
-        size_t st = p == 4 ? spread_stage_bytes<T, 4>(Wa)
-                  : p == 2 ? spread_stage_bytes<T, 2>(Wa) : spread_stage_bytes<T, 1>(Wa);
-        return (p + 1) * bufa + kSpreadWarps * st;
-    };
-    // the autotuner's cap, else NUDIM_TUNE_PLANES, caps the planes per CTA
-    Pa = 4;
+    // adjoint: planes per gather pass 8 (default), 4, 2 or 1 -- the
+    // autotuner's cap, else NUDIM_TUNE_PLANES
+    Pa = 8;
     {
         int v = tune_planes;
         if (!v)
             if (const char *e = getenv("NUDIM_TUNE_PLANES")) v = atoi(e);
-        if (v >= 1 && v < 4) Pa = v >= 2 ? 2 : 1;
+        if (v >= 1 && v < 8) Pa = v >= 4 ? 4 : v >= 2 ? 2 : 1;
     }
-    while (Pa > 1 && spread_smem(Pa) > ((size_t)212 << 10)) Pa /= 2;
-    smem_spread = spread_smem(Pa);
+    const int Wa = 32 / BCa + BCa;
+    smem_spread = kGatherWarps * (Pa == 8   ? gather_stage_bytes<T, 8>(Wa)
+                                  : Pa == 4 ? gather_stage_bytes<T, 4>(Wa)
+                                  : Pa == 2 ? gather_stage_bytes<T, 2>(Wa)
+                                            : gather_stage_bytes<T, 1>(Wa));
+    smem_colifft = 2 * sizeof(C) * fft_buf((size_t)BCa * n0);
     // The limit is a property of the kernel, shared by every plan in the
     // process: set it to the largest size any plan uses (never lower it).
-    const int lim_col = 144 << 10, lim_row = 112 << 10, lim_spread = 212 << 10;
+    const int lim_col = 144 << 10, lim_row = 112 << 10, lim_spread = 96 << 10,
+              lim_colifft = 144 << 10;
     if (rows < 1 || smem_col > (size_t)lim_col || smem_row > (size_t)lim_row ||
-        smem_spread > (size_t)lim_spread) {
+        smem_spread > (size_t)lim_spread || smem_colifft > (size_t)lim_colifft) {
         set_error("fused NFFT: shared memory plan exceeds the kernel limits");
         return NUDIM_EINVAL;
     }
@@ -802,18 +757,21 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     NUDIM_TRY(up((void **)&band_w, L.band_w.data(), sizeof(T) * L.band_w.size()));
     NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     lim_col));
-    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, true, 1>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
-    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, false, 1>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
-    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, true, 2>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
-    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, false, 2>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
-    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, true, 4>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
-    NUDIM_CUDA(cudaFuncSetAttribute(k_spread_colifft<T, false, 4>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_spread));
+    {
+        const void *gk[] = {(const void *)k_spread_gather<T, true, 8>,
+                            (const void *)k_spread_gather<T, false, 8>,
+                            (const void *)k_spread_gather<T, true, 4>,
+                            (const void *)k_spread_gather<T, false, 4>,
+                            (const void *)k_spread_gather<T, true, 2>,
+                            (const void *)k_spread_gather<T, false, 2>,
+                            (const void *)k_spread_gather<T, true, 1>,
+                            (const void *)k_spread_gather<T, false, 1>};
+        for (const void *k : gk)
+            NUDIM_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            lim_spread));
+    }
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colifft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    lim_colifft));
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft<T, PM_COMPLEX>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, lim_row));
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft<T, PM_REAL_INIT>,
@@ -841,10 +799,13 @@ template <typename T> void NfftDev<T>::release_fused()
     fused = false;
 }
 
-template <typename T> int NfftDev<T>::fused_chunk(int nplanes) const
+// Planes per fused pass: the pass's scratch per plane (complex elements:
+// trafo N0*n1 row spectra + smax*M partials, adjoint N0*n1 + n0*n1 grid)
+// within the context's budget.
+template <typename T> int NfftDev<T>::fused_chunk(int nplanes, size_t per_plane) const
 {
-    size_t per = sizeof(C) * ((size_t)N0 * n1 + (size_t)smax * M);
-    size_t budget = ctx->fused_budget ? ctx->fused_budget : ((size_t)1536 << 20);
+    size_t per = sizeof(C) * per_plane;
+    size_t budget = ctx->fused_budget ? ctx->fused_budget : ((size_t)3072 << 20);
     long c = (long)(budget / per);
     if (c < 1) c = 1;
     if (c > nplanes) c = nplanes;
@@ -859,7 +820,7 @@ template <typename T>
 int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia,
                             cudaStream_t st)
 {
-    int chunk = fused_chunk(nplanes);
+    int chunk = fused_chunk(nplanes, (size_t)N0 * n1 + (size_t)smax * M);
     void *wsv;
     size_t nH = (size_t)N0 * n1 * chunk, nP = (size_t)smax * M * chunk;
     NUDIM_TRY(workspace(sizeof(C) * (nH + nP), &wsv));
@@ -906,39 +867,48 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
     return NUDIM_OK;
 }
 
-//   spread    tables + nb*c*(M + N0*n1)   node values in, column spectra out
+//   spread    tables + nb*c*(M + n0*n1)   node values in, grid out
+//   col IFFT  nb*c*(n0*n1 + N0*n1)        grid in, column spectra out
 //   row pass  nb*c*(N0*n1 + 2*N0*N1)      column spectra in, coefficients out
 template <typename T>
 int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca,
                               cudaStream_t st)
 {
-    int chunk = fused_chunk(nplanes);
+    int chunk = fused_chunk(nplanes, (size_t)N0 * n1 + (size_t)n0 * n1);
     void *wsv;
-    size_t nH = (size_t)N0 * n1 * chunk;
-    NUDIM_TRY(workspace(sizeof(C) * (nH + (size_t)smax * M * chunk), &wsv));
-    C *Hp = (C *)wsv;
+    size_t nH = (size_t)N0 * n1 * chunk, nG = (size_t)n0 * n1 * chunk;
+    NUDIM_TRY(workspace(sizeof(C) * (nH + nG), &wsv));
+    C *Hp = (C *)wsv, *G = Hp + nH;
     int logn0 = ilog2(n0), logn1 = ilog2(n1);
     const double c = sizeof(C), tab = (double)M * (8 + 2 * kW * sizeof(T));
     for (int p0 = 0; p0 < nplanes; p0 += chunk) {
         int nb = std::min(chunk, nplanes - p0);
         {
-            ProfScope ps(ctx, PK_SPREAD, st, tab + nb * c * ((double)M + (double)N0 * n1));
-            dim3 g(nblka, ceil_div(nb, Pa));
-            const int thr = 32 * kSpreadWarps;
-#define NUDIM_SPREAD(W, PP)                                                                     \
-    k_spread_colifft<T, W, PP><<<g, thr, smem_spread, st>>>(sa, band_off, band_ord, band_node,  \
-                                                            band_w, nbands, N0, n0, logn0, n1,  \
-                                                            BCa, nb, tw0, p0, Hp)
+            ProfScope ps(ctx, PK_SPREAD, st, tab + nb * c * ((double)M + (double)n0 * n1));
+            dim3 g(ceil_div(ntiles, kGatherTilesPerCta), ceil_div(nb, Pa));
+            const int thr = 32 * kGatherWarps;
+#define NUDIM_GATHER(WT, PP)                                                                    \
+    k_spread_gather<T, WT, PP><<<g, thr, smem_spread, st>>>(sa, band_ord, ntiles, band_off,     \
+                                                            band_node, band_w, nbands, n0, n1,  \
+                                                            BCa, nb, p0, G)
             if (sa.w) {
-                if (Pa == 4) NUDIM_SPREAD(true, 4);
-                else if (Pa == 2) NUDIM_SPREAD(true, 2);
-                else NUDIM_SPREAD(true, 1);
+                if (Pa == 8) NUDIM_GATHER(true, 8);
+                else if (Pa == 4) NUDIM_GATHER(true, 4);
+                else if (Pa == 2) NUDIM_GATHER(true, 2);
+                else NUDIM_GATHER(true, 1);
             } else {
-                if (Pa == 4) NUDIM_SPREAD(false, 4);
-                else if (Pa == 2) NUDIM_SPREAD(false, 2);
-                else NUDIM_SPREAD(false, 1);
+                if (Pa == 8) NUDIM_GATHER(false, 8);
+                else if (Pa == 4) NUDIM_GATHER(false, 4);
+                else if (Pa == 2) NUDIM_GATHER(false, 2);
+                else NUDIM_GATHER(false, 1);
             }
-#undef NUDIM_SPREAD
+#undef NUDIM_GATHER
+            NUDIM_LAUNCH_CHECK();
+        }
+        {
+            ProfScope ps(ctx, PK_SPREAD, st, nb * c * ((double)n0 * n1 + (double)N0 * n1));
+            k_colifft<T><<<dim3(nblka, nb), 256, smem_colifft, st>>>(G, N0, n0, logn0, n1, BCa,
+                                                                      tw0, Hp);
             NUDIM_LAUNCH_CHECK();
         }
         {
@@ -959,8 +929,8 @@ template int NfftDev<double>::init_fused(const NfftTables &, cudaStream_t);
 template int NfftDev<float>::init_fused(const NfftTables &, cudaStream_t);
 
 // NUDIM_CTX_AUTOTUNE: for a geometry not yet tuned in this context, build the
-// fused plan for each trafo column width (4, 2) and planes per spreading CTA
-// (4, 2, 1), time one trafo + adjoint of a batch of planes for each (after one
+// fused plan for each trafo column width (4, 2) and planes per spreading
+// gather pass (8, 4, 2), time one trafo + adjoint of a batch of planes for each (after one
 // untimed pair, CUDA events on the plan's stream), keep the fastest in the
 // context and use it for this plan.  Candidates that build the same plan as
 // an earlier one are not timed again.
@@ -989,7 +959,7 @@ template <typename T> int NfftDev<T>::autotune(const NfftTables &t, cudaStream_t
     int choice_bc = 0, choice_p = 0;
     std::vector<std::pair<int, int>> built;  // (BC, Pa) of the plans already timed
     for (int bcc : {4, 2})
-        for (int pc : {4, 2, 1}) {
+        for (int pc : {8, 4, 2}) {
             if (rc) break;
             NfftDev<T> trial;
             trial.tune_bc = bcc;
@@ -1051,8 +1021,8 @@ template int NfftDev<double>::autotune(const NfftTables &, cudaStream_t);
 template int NfftDev<float>::autotune(const NfftTables &, cudaStream_t);
 template void NfftDev<double>::release_fused();
 template void NfftDev<float>::release_fused();
-template int NfftDev<double>::fused_chunk(int) const;
-template int NfftDev<float>::fused_chunk(int) const;
+template int NfftDev<double>::fused_chunk(int, size_t) const;
+template int NfftDev<float>::fused_chunk(int, size_t) const;
 template int NfftDev<double>::trafo_fused(int, const PadArgs<double> &, const InterpArgs<double> &,
                                           cudaStream_t);
 template int NfftDev<float>::trafo_fused(int, const PadArgs<float> &, const InterpArgs<float> &,

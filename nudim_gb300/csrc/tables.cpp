@@ -444,17 +444,13 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
                 }
             });
     });
-    // per block, its tiles longest list first (the spreading CTA hands
-    // them out in this order)
+    // every tile once, longest list first (ties by tile number): the
+    // spreading gather hands them out in this order
     L->band_ord.resize(ntiles);
-    for (int b = 0; b < nblka; b++) {
-        int *o = &L->band_ord[(size_t)b * nb];
-        for (int v = 0; v < nb; v++) o[v] = v;
-        const int *c = &cnt[(size_t)b * nb];
-        std::stable_sort(o, o + nb, [&](int x, int y) {
-            return c[x + 1] - c[x] > c[y + 1] - c[y];
-        });
-    }
+    for (size_t i = 0; i < ntiles; i++) L->band_ord[i] = (int)i;
+    std::stable_sort(L->band_ord.begin(), L->band_ord.end(), [&](int x, int y) {
+        return cnt[(size_t)x + 1] - cnt[x] > cnt[(size_t)y + 1] - cnt[y];
+    });
     return 0;
 }
 

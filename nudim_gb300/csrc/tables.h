@@ -63,7 +63,7 @@ template <typename W> struct FusedLists {
     HostArray<W> ent_qa, ent_q1;
     std::vector<int> band_off, band_node;   // CSR over tiles b * nbands + v
     HostArray<W> band_w;                    // per entry R row + BCa column weights
-    std::vector<int> band_ord;              // per block its tiles, longest list first
+    std::vector<int> band_ord;              // every tile once, longest list first
 };
 
 // BC a power of two dividing n1; BCa a power of two <= 32 dividing n1.

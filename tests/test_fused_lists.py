@@ -77,11 +77,15 @@ static int check(int N, int M, int BC, bool pair_rows, unsigned seed)
     // ---- adjoint tile entries
     const int R = L.R, Wn = R + L.BCa, nb = L.nbands;
     std::vector<std::map<long, double>> ad(M);
-    for (int b = 0; b < L.nblka; b++) {
+    {
+        const size_t ntiles = (size_t)L.nblka * nb;
+        if (L.band_ord.size() != ntiles) return 42;
+        std::vector<int> once(ntiles, 0);
         int prev_len = 1 << 30;
-        for (int k = 0; k < nb; k++) {
-            int v = L.band_ord[(size_t)b * nb + k];
-            int tile = b * nb + v, lo = L.band_off[tile], hi = L.band_off[tile + 1];
+        for (size_t k = 0; k < ntiles; k++) {
+            int tile = L.band_ord[k];
+            if (tile < 0 || (size_t)tile >= ntiles || once[tile]++) return 43;  // each tile once
+            int b = tile / nb, v = tile - b * nb, lo = L.band_off[tile], hi = L.band_off[tile + 1];
             if (hi - lo > prev_len) return 40;     // longest first
             prev_len = hi - lo;
             for (int e = lo; e < hi; e++) {
