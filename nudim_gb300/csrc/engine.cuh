@@ -169,14 +169,15 @@ template <typename T> struct NfftDev {
     bool fused = false;
     int BC = 0, nblk = 0, smax = 0, rows = 4;    // trafo column blocks
     int BCa = 0, nblka = 0, nbands = 0, ntiles = 0;  // adjoint column blocks and tiles
+    int nunits = 0, nfix = 0, nextra = 0;  // spreading work units, split tiles, extra ranges
+    int4 *units = nullptr, *fixups = nullptr;
     int Pa = 1;                                     // planes per spreading-gather pass
     // caps on the trafo column width and the planes per spreading CTA for
     // init_fused (0: the defaults, or the NUDIM_TUNE_* environment knobs)
     int tune_bc = 0, tune_planes = 0;
     size_t smem_col = 0, smem_row = 0, smem_spread = 0, smem_colifft = 0;
     C *tw0 = nullptr, *tw1 = nullptr;
-    int *blk_off = nullptr, *ent = nullptr, *band_off = nullptr, *band_node = nullptr,
-        *band_ord = nullptr;
+    int *blk_off = nullptr, *ent = nullptr, *band_off = nullptr, *band_node = nullptr;
     T *band_w = nullptr;            // per adjoint tile entry: R row + BCa column weights
     int nE = 0;                     // trafo entries; their records (structure of arrays):
     int *e_rb = nullptr, *e_cc = nullptr;

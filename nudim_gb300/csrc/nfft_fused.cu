@@ -18,6 +18,7 @@
 //
 // No atomics: every output element has exactly one writer, and every sum
 // has a fixed order, so results are deterministic.
+#include <algorithm>
 #include <cstdlib>
 #include <type_traits>
 
@@ -419,12 +420,17 @@ k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ 
 // across chunks; FP64: fused multiply-adds in ascending node order.  The tile's 32 points of each plane are one
 // contiguous 256-byte (FP32) store: G is laid out column block by column
 // block, [plane][block][row][column in block], which is also the order the
-// column IFFT reads.  Tiles come in one global order, longest list first;
-// a CTA takes kGatherTilesPerCta consecutive tiles of it and its warps
-// share them out through a shared counter.  No grid point has two writers
-// and every sum has a fixed order: the results are deterministic.
+// column IFFT reads.  The work units are ranges of at most kGatherMaxEntries
+// entries of a tile's list (the lists near the polar grid's centre run to
+// over a thousand entries; a whole list per warp would make the longest one
+// the kernel's critical path): a tile's first range writes G, its later
+// ranges write partial sums that k_spread_fixup adds in range order.  Units
+// come longest first; a CTA takes kGatherUnitsPerCta consecutive ones and
+// its warps share them out through a shared counter.  No grid point has two
+// writers and every sum has a fixed order: the results are deterministic.
 constexpr int kGatherWarps = 8;
-constexpr int kGatherTilesPerCta = 32;
+constexpr int kGatherUnitsPerCta = 16;
+constexpr int kGatherMaxEntries = 128;
 
 // node values of a stage: row stride in complex elements (padded so the
 // lanes' 16-byte staging stores meet distinct banks)
@@ -436,10 +442,10 @@ template <typename T, int P> __host__ __device__ constexpr size_t gather_stage_b
 
 template <typename T, bool WEIGHTED, int P>
 __global__ void __launch_bounds__(32 * kGatherWarps)
-k_spread_gather(SpreadArgs<T> sa, const int *__restrict__ tile_ord, int ntiles,
-                const int *__restrict__ band_off, const int *__restrict__ band_node,
-                const T *__restrict__ band_w, int nbands, int n0, int n1, int BC,
-                int nb_planes, int plane0, cplx_t<T> *__restrict__ G)
+k_spread_gather(SpreadArgs<T> sa, const int4 *__restrict__ units, int nunits,
+                const int *__restrict__ band_node, const T *__restrict__ band_w, int nbands,
+                int n0, int n1, int BC, int nb_planes, int plane0, cplx_t<T> *__restrict__ G,
+                cplx_t<T> *__restrict__ part)
 {
     using C = cplx_t<T>;
     constexpr int FS = gather_fs_stride<P>();
@@ -450,16 +456,16 @@ k_spread_gather(SpreadArgs<T> sa, const int *__restrict__ tile_ord, int ntiles,
     T *ws = (T *)(smraw + warp * gather_stage_bytes<T, P>(W));  // [32][W] weights
     C *fs = (C *)(ws + 32 * W);                                 // [32][FS] node values
     const int pb = blockIdx.y * P, np = min(P, nb_planes - pb);
-    const int t0 = blockIdx.x * kGatherTilesPerCta;
-    const int t1 = min(ntiles, t0 + kGatherTilesPerCta);
+    const int t0 = blockIdx.x * kGatherUnitsPerCta;
+    const int t1 = min(nunits, t0 + kGatherUnitsPerCta);
     if (threadIdx.x == 0) next_tile = t0 + kGatherWarps;
     __syncthreads();
     const int rr = lane / BC, cc = lane - rr * BC;
     const int wv16 = W * (int)sizeof(T) / 16;  // 16-byte vectors of an entry's weights
     int it = t0 + warp;
     while (it < t1) {
-        const int tile = tile_ord[it];
-        const int beg = band_off[tile], end = band_off[tile + 1];
+        const int4 un = units[it];  // tile, first entry, end, partial slot (0: G)
+        const int tile = un.x, beg = un.y, end = un.z;
         T ar[P], ai[P];
         Comp<T> kr[P], ki[P];
 #pragma unroll
@@ -540,14 +546,47 @@ k_spread_gather(SpreadArgs<T> sa, const int *__restrict__ tile_ord, int ntiles,
                     ar[p] = kr[p].value();
                     ai[p] = ki[p].value();
                 }
-                G[(((size_t)(pb + p) * nblk + b) * n0 + (size_t)v * R) * BC + lane] =
-                    mkc<T>(ar[p], ai[p]);
+                const C val = mkc<T>(ar[p], ai[p]);
+                if (un.w == 0)
+                    G[(((size_t)(pb + p) * nblk + b) * n0 + (size_t)v * R) * BC + lane] = val;
+                else
+                    part[(((size_t)(un.w - 1) * nb_planes) + pb + p) * 32 + lane] = val;
             }
         }
         int nt = 0;
         if (lane == 0) nt = atomicAdd(&next_tile, 1);
         it = __shfl_sync(0xffffffffu, nt, 0);
     }
+}
+
+// The tiles whose lists were split into several ranges: their grid points
+// get the later ranges' partial sums added in range order (FP32: Neumaier
+// compensated).  fix[i] = {tile, first partial slot, number of slots}; one
+// thread per (grid point of the tile, plane).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_spread_fixup(const int4 *__restrict__ fix, int nbands, int n0, int n1, int BC,
+               int nb_planes, const cplx_t<T> *__restrict__ part, cplx_t<T> *__restrict__ G)
+{
+    using C = cplx_t<T>;
+    const int4 fx = fix[blockIdx.x];
+    const int lane = threadIdx.x & 31, R = 32 / BC, nblk = n1 / BC;
+    const int p = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (p >= nb_planes) return;
+    const int b = fx.x / nbands, v = fx.x - b * nbands;
+    C *g = G + (((size_t)p * nblk + b) * n0 + (size_t)v * R) * BC + lane;
+    Comp<T> kr, ki;
+    kr.init();
+    ki.init();
+    const C g0 = *g;
+    kr.add(g0.x);
+    ki.add(g0.y);
+    for (int k = 0; k < fx.z; k++) {
+        const C q = part[(((size_t)(fx.y - 1 + k) * nb_planes) + p) * 32 + lane];
+        kr.add(q.x);
+        ki.add(q.y);
+    }
+    *g = mkc<T>(kr.value(), ki.value());
 }
 
 // ================================================================ K4b column IFFT
@@ -701,6 +740,26 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     nblka = L.nblka;
     nbands = L.nbands;
     ntiles = nblka * nbands;
+    // spreading work units: every tile's list in ranges of at most
+    // kGatherMaxEntries entries (split evenly), longest range first; the
+    // tiles of more than one range, with their partial slots, for the fix-up
+    std::vector<int4> hu, hf;
+    nextra = 0;
+    for (int i = 0; i < ntiles; i++) {
+        const int t = L.band_ord[i], b0 = L.band_off[t], len = L.band_off[t + 1] - b0;
+        const int nr = std::max(1, ceil_div(len, kGatherMaxEntries));
+        for (int r = 0; r < nr; r++)
+            hu.push_back(make_int4(t, b0 + (int)((long)len * r / nr),
+                                   b0 + (int)((long)len * (r + 1) / nr), r ? nextra + r : 0));
+        if (nr > 1) {
+            hf.push_back(make_int4(t, nextra + 1, nr - 1, 0));
+            nextra += nr - 1;
+        }
+    }
+    std::stable_sort(hu.begin(), hu.end(),
+                     [](const int4 &a, const int4 &b) { return a.z - a.y > b.z - b.y; });
+    nunits = (int)hu.size();
+    nfix = (int)hf.size();
     // rows per CTA in the row passes: two (padded) rows x n1 complex buffers within 112 KB
     rows = 4;
     while (rows > 1 && 2 * sizeof(C) * fft_buf((size_t)rows * t.n1) > ((size_t)112 << 10)) rows--;
@@ -753,7 +812,8 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     NUDIM_TRY(up((void **)&band_off, L.band_off.data(), sizeof(int) * L.band_off.size()));
     NUDIM_TRY(up((void **)&band_node, L.band_node.data(),
                  sizeof(int) * std::max<size_t>(1, L.band_node.size())));
-    NUDIM_TRY(up((void **)&band_ord, L.band_ord.data(), sizeof(int) * L.band_ord.size()));
+    NUDIM_TRY(up((void **)&units, hu.data(), sizeof(int4) * hu.size()));
+    if (!hf.empty()) NUDIM_TRY(up((void **)&fixups, hf.data(), sizeof(int4) * hf.size()));
     NUDIM_TRY(up((void **)&band_w, L.band_w.data(), sizeof(T) * L.band_w.size()));
     NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     lim_col));
@@ -788,12 +848,13 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
 
 template <typename T> void NfftDev<T>::release_fused()
 {
-    void *ptrs[] = {tw0,      tw1,       blk_off,  ent,    nslots, band_off, band_node,
-                    band_ord, band_w, e_rb, e_cc, e_qa, e_q1};
+    void *ptrs[] = {tw0,    tw1,  blk_off, ent,  nslots, band_off, band_node,
+                    units,  band_w, e_rb, e_cc, e_qa, e_q1, fixups};
     for (void *q : ptrs)
         if (q) cudaFreeAsync(q, ast);
     tw0 = tw1 = nullptr;
-    blk_off = ent = band_off = band_node = band_ord = e_rb = e_cc = nullptr;
+    blk_off = ent = band_off = band_node = e_rb = e_cc = nullptr;
+    units = fixups = nullptr;
     band_w = e_qa = e_q1 = nullptr;
     nslots = nullptr;
     fused = false;
@@ -874,23 +935,23 @@ template <typename T>
 int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca,
                               cudaStream_t st)
 {
-    int chunk = fused_chunk(nplanes, (size_t)N0 * n1 + (size_t)n0 * n1);
+    int chunk = fused_chunk(nplanes, (size_t)N0 * n1 + (size_t)n0 * n1 + 32 * (size_t)nextra);
     void *wsv;
     size_t nH = (size_t)N0 * n1 * chunk, nG = (size_t)n0 * n1 * chunk;
-    NUDIM_TRY(workspace(sizeof(C) * (nH + nG), &wsv));
-    C *Hp = (C *)wsv, *G = Hp + nH;
+    NUDIM_TRY(workspace(sizeof(C) * (nH + nG + 32 * (size_t)nextra * chunk), &wsv));
+    C *Hp = (C *)wsv, *G = Hp + nH, *part = G + nG;
     int logn0 = ilog2(n0), logn1 = ilog2(n1);
     const double c = sizeof(C), tab = (double)M * (8 + 2 * kW * sizeof(T));
     for (int p0 = 0; p0 < nplanes; p0 += chunk) {
         int nb = std::min(chunk, nplanes - p0);
         {
             ProfScope ps(ctx, PK_SPREAD, st, tab + nb * c * ((double)M + (double)n0 * n1));
-            dim3 g(ceil_div(ntiles, kGatherTilesPerCta), ceil_div(nb, Pa));
+            dim3 g(ceil_div(nunits, kGatherUnitsPerCta), ceil_div(nb, Pa));
             const int thr = 32 * kGatherWarps;
 #define NUDIM_GATHER(WT, PP)                                                                    \
-    k_spread_gather<T, WT, PP><<<g, thr, smem_spread, st>>>(sa, band_ord, ntiles, band_off,     \
-                                                            band_node, band_w, nbands, n0, n1,  \
-                                                            BCa, nb, p0, G)
+    k_spread_gather<T, WT, PP><<<g, thr, smem_spread, st>>>(sa, units, nunits, band_node,       \
+                                                            band_w, nbands, n0, n1, BCa, nb,    \
+                                                            p0, G, part)
             if (sa.w) {
                 if (Pa == 8) NUDIM_GATHER(true, 8);
                 else if (Pa == 4) NUDIM_GATHER(true, 4);
@@ -904,6 +965,11 @@ int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropAr
             }
 #undef NUDIM_GATHER
             NUDIM_LAUNCH_CHECK();
+            if (nfix > 0) {
+                k_spread_fixup<T><<<dim3(nfix, ceil_div(nb, 8)), 256, 0, st>>>(
+                    fixups, nbands, n0, n1, BCa, nb, part, G);
+                NUDIM_LAUNCH_CHECK();
+            }
         }
         {
             ProfScope ps(ctx, PK_SPREAD, st, nb * c * ((double)n0 * n1 + (double)N0 * n1));
