@@ -589,6 +589,127 @@ k_spread_fixup(const int4 *__restrict__ fix, int nbands, int n0, int n1, int BC,
     *g = mkc<T>(kr.value(), ki.value());
 }
 
+// ================================================================ four-step register FFT
+// n = R1 x R2 points with one shared-memory exchange: input index l = j +
+// R2 m (j < R2, m < R1), pass 1 an R1-point DFT over m per j (registers),
+// twiddle W_n^{j k1}, exchange, pass 2 an R2-point DFT over j per k1, output
+// index k = k1 + R1 k2 (the classical four-step factorisation of the DFT).
+// R = 32 DFTs in registers split as two 16-point DFTs (dft_regs<16>) and a
+// radix-2 step with the twiddles W_32^p.
+template <typename T, int DIR> __device__ __forceinline__ cplx_t<T> w32(int p)
+{
+    // cos(2 pi p / 32), p = 0..8
+    constexpr double c[9] = {1.0,
+                             0.98078528040323044913,
+                             0.92387953251128675613,
+                             0.83146961230254523708,
+                             0.70710678118654752440,
+                             0.55557023301960222474,
+                             0.38268343236508977173,
+                             0.19509032201612826785,
+                             0.0};
+    const int q = p & 7, h = p >> 3;  // p = 8h + q: rotate by h quarter turns
+    double cs, sn;
+    const double cq = c[q], sq = c[8 - q];
+    switch (h & 3) {
+    case 0: cs = cq; sn = sq; break;
+    case 1: cs = -sq; sn = cq; break;
+    case 2: cs = -cq; sn = -sq; break;
+    default: cs = sq; sn = -cq; break;
+    }
+    return mkc<T>((T)cs, (T)(DIR * sn));
+}
+
+// R-point DFT (R = 16 or 32) of a[0..R) in registers; X[p] is left in
+// a[fs_out<R>(p)].
+template <int R> __device__ __forceinline__ constexpr int fs_out(int p)
+{
+    return R == 16 ? dft_out<16>(p) : (p < 16 ? 2 * dft_out<16>(p) : 2 * dft_out<16>(p - 16) + 1);
+}
+
+template <typename T, int DIR, int R> __device__ __forceinline__ void fs_dft(cplx_t<T> *a)
+{
+    using C = cplx_t<T>;
+    if constexpr (R == 16) {
+        dft_regs<T, DIR, 16>(a);
+    } else {
+        C e[16], o[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            e[u] = a[2 * u];
+            o[u] = a[2 * u + 1];
+        }
+        dft_regs<T, DIR, 16>(e);
+        dft_regs<T, DIR, 16>(o);
+        // X[p] = E[p] + W32^p O[p], X[p + 16] = E[p] - W32^p O[p]
+#pragma unroll
+        for (int p = 0; p < 16; p++) {
+            const C ev = e[dft_out<16>(p)];
+            C ov = o[dft_out<16>(p)];
+            if (p) ov = cmul<T>(ov, w32<T, DIR>(p));
+            a[2 * dft_out<16>(p)] = mkc<T>(ev.x + ov.x, ev.y + ov.y);
+            a[2 * dft_out<16>(p) + 1] = mkc<T>(ev.x - ov.x, ev.y - ov.y);
+        }
+    }
+}
+
+// ================================================================ K4b' column IFFT, four-step
+// The column IFFT for n0 = R1 x R2 (256, 512, 1024): one CTA per (column
+// block of 4 columns, plane), R2 threads per column.  Pass 1 reads the grid
+// straight from G into registers (a warp reads 8 rows x 4 columns, 256
+// contiguous bytes, per step), the exchange goes through shared memory
+// (column stride padded so neither pass meets a bank twice), pass 2 writes
+// the N0 kept rows to H'.
+template <int R1, int R2> __host__ __device__ constexpr int fs_col_stride()
+{
+    // R1 x (R2 + 1) rounded up to 4 mod 16 elements
+    return ((R1 * (R2 + 1) + 11) / 16) * 16 + 4;
+}
+
+template <typename T, int R1, int R2>
+__global__ void __launch_bounds__(4 * R2)
+k_colifft_fs(const cplx_t<T> *__restrict__ G, int N0, int n1, const cplx_t<T> *__restrict__ tw0,
+             cplx_t<T> *__restrict__ Hp)
+{
+    using C = cplx_t<T>;
+    constexpr int n0 = R1 * R2, BC = 4, CS = fs_col_stride<R1, R2>();
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *S = (C *)smraw;  // [column][k1][j], column stride CS, row stride R2 + 1
+    const int cb = blockIdx.x, b = blockIdx.y, nblk = n1 / BC;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = lane & 3, j = warp * 8 + (lane >> 2);
+    const C *Gb = G + ((size_t)b * nblk + cb) * n0 * BC;
+    {
+        C a[R1];
+#pragma unroll
+        for (int m = 0; m < R1; m++) a[m] = Gb[(size_t)(j + R2 * m) * BC + c];
+        fs_dft<T, +1, R1>(a);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) {
+            C v = a[fs_out<R1>(k1)];
+            if (k1) {
+                C w = tw0[j * k1];
+                w.y = -w.y;  // inverse: e^{+2 pi i j k1 / n0}
+                v = cmul<T>(v, w);
+            }
+            S[c * CS + k1 * (R2 + 1) + j] = v;
+        }
+    }
+    __syncthreads();
+    C *Hb = Hp + (size_t)b * N0 * n1 + (size_t)cb * BC + c;
+    for (int k1 = j; k1 < R1; k1 += R2) {
+        C y[R2];
+#pragma unroll
+        for (int jj = 0; jj < R2; jj++) y[jj] = S[c * CS + k1 * (R2 + 1) + jj];
+        fs_dft<T, +1, R2>(y);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; k2++) {
+            const int a = (k1 + R1 * k2 + N0 / 2) & (n0 - 1);
+            if (a < N0) Hb[(size_t)a * n1] = y[fs_out<R2>(k2)];
+        }
+    }
+}
+
 // ================================================================ K4b column IFFT
 // One CTA per (column block, plane): the block's n0 x BC grid values (one
 // contiguous run of G) into shared memory column by column, BC inverse
@@ -832,6 +953,16 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     }
     NUDIM_CUDA(cudaFuncSetAttribute(k_colifft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     lim_colifft));
+    // the four-step column IFFTs' exchange buffers (FP64 1024 points: 68 KB)
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colifft_fs<T, 32, 32>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(C) * 4 * fs_col_stride<32, 32>())));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colifft_fs<T, 32, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(C) * 4 * fs_col_stride<32, 16>())));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colifft_fs<T, 16, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(C) * 4 * fs_col_stride<16, 16>())));
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft<T, PM_COMPLEX>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, lim_row));
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft<T, PM_REAL_INIT>,
@@ -973,8 +1104,19 @@ int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropAr
         }
         {
             ProfScope ps(ctx, PK_SPREAD, st, nb * c * ((double)n0 * n1 + (double)N0 * n1));
-            k_colifft<T><<<dim3(nblka, nb), 256, smem_colifft, st>>>(G, N0, n0, logn0, n1, BCa,
-                                                                      tw0, Hp);
+            const size_t smem_fs =
+                sizeof(C) * 4 *
+                (n0 == 1024 ? fs_col_stride<32, 32>() : n0 == 512 ? fs_col_stride<32, 16>()
+                                                                  : fs_col_stride<16, 16>());
+            if (BCa == 4 && n0 == 1024)
+                k_colifft_fs<T, 32, 32><<<dim3(nblka, nb), 128, smem_fs, st>>>(G, N0, n1, tw0, Hp);
+            else if (BCa == 4 && n0 == 512)
+                k_colifft_fs<T, 32, 16><<<dim3(nblka, nb), 64, smem_fs, st>>>(G, N0, n1, tw0, Hp);
+            else if (BCa == 4 && n0 == 256)
+                k_colifft_fs<T, 16, 16><<<dim3(nblka, nb), 64, smem_fs, st>>>(G, N0, n1, tw0, Hp);
+            else
+                k_colifft<T><<<dim3(nblka, nb), 256, smem_colifft, st>>>(G, N0, n0, logn0, n1,
+                                                                          BCa, tw0, Hp);
             NUDIM_LAUNCH_CHECK();
         }
         {
