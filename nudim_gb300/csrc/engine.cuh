@@ -167,7 +167,8 @@ template <typename T> struct NfftDev {
 
     // fused path (nfft_fused.cu): no oversampled grid in HBM
     bool fused = false;
-    int BC = 0, nblk = 0, smax = 0, rows = 4;    // trafo column blocks
+    int BC = 0, nblk = 0, smax = 0, rows = 4;    // trafo column blocks; rows per row-pass CTA
+    bool row_fs = false;                         // row passes as four-step FFTs
     int BCa = 0, nblka = 0, nbands = 0, ntiles = 0;  // adjoint column blocks and tiles
     int nunits = 0, nfix = 0, nextra = 0;  // spreading work units, split tiles, extra ranges
     int4 *units = nullptr, *fixups = nullptr;

@@ -200,6 +200,76 @@ __device__ cplx_t<T> *block_fft(cplx_t<T> *a, cplx_t<T> *b, int n, int logn, int
 }
 
 
+// ================================================================ four-step register FFT
+// n = R1 x R2 points with one shared-memory exchange: input index l = j +
+// R2 m (j < R2, m < R1), pass 1 an R1-point DFT over m per j (registers),
+// twiddle W_n^{j k1}, exchange, pass 2 an R2-point DFT over j per k1, output
+// index k = k1 + R1 k2 (the classical four-step factorisation of the DFT).
+// R = 32 DFTs in registers split as two 16-point DFTs (dft_regs<16>) and a
+// radix-2 step with the twiddles W_32^p.
+template <typename T, int DIR> __device__ __forceinline__ cplx_t<T> w32(int p)
+{
+    // cos(2 pi p / 32), p = 0..8
+    constexpr double c[9] = {1.0,
+                             0.98078528040323044913,
+                             0.92387953251128675613,
+                             0.83146961230254523708,
+                             0.70710678118654752440,
+                             0.55557023301960222474,
+                             0.38268343236508977173,
+                             0.19509032201612826785,
+                             0.0};
+    const int q = p & 7, h = p >> 3;  // p = 8h + q: rotate by h quarter turns
+    double cs, sn;
+    const double cq = c[q], sq = c[8 - q];
+    switch (h & 3) {
+    case 0: cs = cq; sn = sq; break;
+    case 1: cs = -sq; sn = cq; break;
+    case 2: cs = -cq; sn = -sq; break;
+    default: cs = sq; sn = -cq; break;
+    }
+    return mkc<T>((T)cs, (T)(DIR * sn));
+}
+
+// R-point DFT (R = 16 or 32) of a[0..R) in registers; X[p] is left in
+// a[fs_out<R>(p)].
+template <int R> __device__ __forceinline__ constexpr int fs_out(int p)
+{
+    return R == 16 ? dft_out<16>(p) : (p < 16 ? 2 * dft_out<16>(p) : 2 * dft_out<16>(p - 16) + 1);
+}
+
+template <typename T, int DIR, int R> __device__ __forceinline__ void fs_dft(cplx_t<T> *a)
+{
+    using C = cplx_t<T>;
+    if constexpr (R == 16) {
+        dft_regs<T, DIR, 16>(a);
+    } else {
+        C e[16], o[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            e[u] = a[2 * u];
+            o[u] = a[2 * u + 1];
+        }
+        dft_regs<T, DIR, 16>(e);
+        dft_regs<T, DIR, 16>(o);
+        // X[p] = E[p] + W32^p O[p], X[p + 16] = E[p] - W32^p O[p]
+#pragma unroll
+        for (int p = 0; p < 16; p++) {
+            const C ev = e[dft_out<16>(p)];
+            C ov = o[dft_out<16>(p)];
+            if (p) ov = cmul<T>(ov, w32<T, DIR>(p));
+            a[2 * dft_out<16>(p)] = mkc<T>(ev.x + ov.x, ev.y + ov.y);
+            a[2 * dft_out<16>(p) + 1] = mkc<T>(ev.x - ov.x, ev.y - ov.y);
+        }
+    }
+}
+
+template <int R1, int R2> __host__ __device__ constexpr int fs_col_stride()
+{
+    // R1 x (R2 + 1) rounded up to 4 mod 16 elements
+    return ((R1 * (R2 + 1) + 11) / 16) * 16 + 4;
+}
+
 // ================================================================ K1 row pass (trafo)
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256)
@@ -321,6 +391,98 @@ k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int 
             T sr = 0, si = 0;
             if constexpr (sizeof(T) == 4) {
                 // FP32 form: one paired FMA per row, (re, im) += q * g
+                float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    float4 pr = *(const float4 *)(gp + ((rb + 2 * i) & m0));
+                    s2 = __ffma2_rn(make_float2(qa[2 * i], qa[2 * i]), make_float2(pr.x, pr.y), s2);
+                    s2 = __ffma2_rn(make_float2(qa[2 * i + 1], qa[2 * i + 1]),
+                                    make_float2(pr.z, pr.w), s2);
+                }
+                sr = s2.x;
+                si = s2.y;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    C g = gp[(rb + i) & m0];
+                    sr += qa[i] * g.x;
+                    si += qa[i] * g.y;
+                }
+            }
+            T w = e_q1[(size_t)q * nE + e];
+            ar += w * sr;
+            ai += w * si;
+        }
+        part[((size_t)b * smax + (js & 7)) * M + (js >> 3)] = mkc<T>(ar, ai);
+    }
+}
+
+// ================================================================ K2' column pass, four-step
+// k_colfft_interp with the column FFTs as four-step register FFTs (n0 =
+// R1 x R2, BC = 4): the first 4 R2 threads read the block's N0 nonzero rows
+// of H straight into pass 1's registers (a warp reads 8 rows x 4 columns
+// per step), exchange through shared memory, and pass 2 writes the columns
+// to Gs (column stride n0 + 8: the four columns' stores meet distinct
+// banks); then every thread interpolates as in k_colfft_interp.
+template <typename T, int R1, int R2>
+__global__ void __launch_bounds__(32 * col_warps<T>(), sizeof(T) == 4 ? NUDIM_COL_MINB : 1)
+k_colfft_interp_fs(const cplx_t<T> *__restrict__ H, int N0, int n1,
+                   const cplx_t<T> *__restrict__ tw0, const int *__restrict__ blk_off,
+                   const int *__restrict__ ent, const int *__restrict__ e_rb,
+                   const int *__restrict__ e_cc, const T *__restrict__ e_qa,
+                   const T *__restrict__ e_q1, int nE, int M, int smax,
+                   cplx_t<T> *__restrict__ part)
+{
+    using C = cplx_t<T>;
+    constexpr int n0 = R1 * R2, BC = 4, GS = n0 + 8, CS = fs_col_stride<R1, R2>();
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *Gs = (C *)smraw, *S = Gs + BC * GS;
+    const int cb = blockIdx.x, b = blockIdx.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool fft = threadIdx.x < 4 * R2;
+    const int c = lane & 3, j = warp * 8 + (lane >> 2);
+    if (fft) {
+        const C *Hb = H + (size_t)b * N0 * n1 + (size_t)cb * BC + c;
+        C x[R1];
+#pragma unroll
+        for (int m = 0; m < R1; m++) {
+            const int l0 = j + R2 * m;
+            const int a = (l0 < n0 / 2 ? l0 : l0 - n0) + N0 / 2;
+            x[m] = (a >= 0 && a < N0) ? Hb[(size_t)a * n1] : mkc<T>(0, 0);
+        }
+        fs_dft<T, -1, R1>(x);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) {
+            C v = x[fs_out<R1>(k1)];
+            if (k1) v = cmul<T>(v, tw0[j * k1]);
+            S[c * CS + k1 * (R2 + 1) + j] = v;
+        }
+    }
+    __syncthreads();
+    if (fft) {
+        for (int k1 = j; k1 < R1; k1 += R2) {
+            C y[R2];
+#pragma unroll
+            for (int jj = 0; jj < R2; jj++) y[jj] = S[c * CS + k1 * (R2 + 1) + jj];
+            fs_dft<T, -1, R2>(y);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; k2++) Gs[c * GS + k1 + R1 * k2] = y[fs_out<R2>(k2)];
+        }
+    }
+    __syncthreads();
+    const int beg = blk_off[cb], end = blk_off[cb + 1];
+    const int m0 = n0 - 1;
+    for (int e = beg + threadIdx.x; e < end; e += blockDim.x) {
+        const int js = ent[e], rb = e_rb[e], ccn = e_cc[e];
+        const int cl0 = ccn & 255, cnt = ccn >> 8;
+        T qa[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) qa[i] = e_qa[(size_t)i * nE + e];
+        T ar = 0, ai = 0;
+        for (int q = 0; q < cnt; q++) {
+            const C *gp = Gs + (size_t)((cl0 + q) & (BC - 1)) * GS;
+            T sr = 0, si = 0;
+            if constexpr (sizeof(T) == 4) {
                 float2 s2 = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int i = 0; i < 8; i++) {
@@ -589,67 +751,126 @@ k_spread_fixup(const int4 *__restrict__ fix, int nbands, int n0, int n1, int BC,
     *g = mkc<T>(kr.value(), ki.value());
 }
 
-// ================================================================ four-step register FFT
-// n = R1 x R2 points with one shared-memory exchange: input index l = j +
-// R2 m (j < R2, m < R1), pass 1 an R1-point DFT over m per j (registers),
-// twiddle W_n^{j k1}, exchange, pass 2 an R2-point DFT over j per k1, output
-// index k = k1 + R1 k2 (the classical four-step factorisation of the DFT).
-// R = 32 DFTs in registers split as two 16-point DFTs (dft_regs<16>) and a
-// radix-2 step with the twiddles W_32^p.
-template <typename T, int DIR> __device__ __forceinline__ cplx_t<T> w32(int p)
-{
-    // cos(2 pi p / 32), p = 0..8
-    constexpr double c[9] = {1.0,
-                             0.98078528040323044913,
-                             0.92387953251128675613,
-                             0.83146961230254523708,
-                             0.70710678118654752440,
-                             0.55557023301960222474,
-                             0.38268343236508977173,
-                             0.19509032201612826785,
-                             0.0};
-    const int q = p & 7, h = p >> 3;  // p = 8h + q: rotate by h quarter turns
-    double cs, sn;
-    const double cq = c[q], sq = c[8 - q];
-    switch (h & 3) {
-    case 0: cs = cq; sn = sq; break;
-    case 1: cs = -sq; sn = cq; break;
-    case 2: cs = -cq; sn = -sq; break;
-    default: cs = sq; sn = -cq; break;
-    }
-    return mkc<T>((T)cs, (T)(DIR * sn));
-}
+// ================================================================ K1'/K5' row passes, four-step
+// The row passes for n1 = R1 x R2 (256, 512, 1024): R2 threads per row,
+// 128 / R2 rows per 128-thread CTA, each row's exchange buffer R1 x (R2 + 1)
+// elements.  K1': deconvolve + zero-pad the N1 coefficients of the row
+// straight into pass 1's registers (only the nonzero ones are loaded),
+// forward FFT, all n1 outputs to H.  K5': the row of H' into registers,
+// inverse FFT, the N1 kept outputs deconvolved into the coefficients plus
+// the epilogue (|z|^2 partial per CTA, p = z).
+template <int R1, int R2> __host__ __device__ constexpr int fs_row_stride() { return R1 * (R2 + 1); }
 
-// R-point DFT (R = 16 or 32) of a[0..R) in registers; X[p] is left in
-// a[fs_out<R>(p)].
-template <int R> __device__ __forceinline__ constexpr int fs_out(int p)
-{
-    return R == 16 ? dft_out<16>(p) : (p < 16 ? 2 * dft_out<16>(p) : 2 * dft_out<16>(p - 16) + 1);
-}
-
-template <typename T, int DIR, int R> __device__ __forceinline__ void fs_dft(cplx_t<T> *a)
+template <typename T, int MODE, int R1, int R2>
+__global__ void __launch_bounds__(128)
+k_rowfft_fs(const void *__restrict__ src, size_t src_stride, int N0, int N1,
+            const T *__restrict__ c0, const T *__restrict__ c1, const cplx_t<T> *__restrict__ tw1,
+            int plane0, cplx_t<T> *__restrict__ H, cplx_t<T> *__restrict__ f_init, size_t f_stride)
 {
     using C = cplx_t<T>;
-    if constexpr (R == 16) {
-        dft_regs<T, DIR, 16>(a);
-    } else {
-        C e[16], o[16];
+    constexpr int n1 = R1 * R2, RPC = 128 / R2;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int line = threadIdx.x / R2, j = threadIdx.x - line * R2;
+    C *S = (C *)smraw + line * fs_row_stride<R1, R2>();
+    const int b = blockIdx.y, gb = plane0 + b, a = blockIdx.x * RPC + line;
+    const bool live = a < N0;
+    C x[R1];
+    const T ca = live ? c0[a] : T(0);
 #pragma unroll
-        for (int u = 0; u < 16; u++) {
-            e[u] = a[2 * u];
-            o[u] = a[2 * u + 1];
+    for (int m = 0; m < R1; m++) {
+        const int l = j + R2 * m;
+        const int k1 = l < n1 / 2 ? l : l - n1, c = k1 + N1 / 2;
+        x[m] = mkc<T>(0, 0);
+        if (live && c >= 0 && c < N1) {
+            const size_t o = (size_t)gb * src_stride + (size_t)a * N1 + c;
+            C sv;
+            if (MODE == PM_COMPLEX) {
+                sv = ((const C *)src)[o];
+            } else {
+                sv = mkc<T>(((const T *)src)[o], T(0));
+                f_init[(size_t)gb * f_stride + (size_t)a * N1 + c] = sv;
+            }
+            const T sc = ca * c1[c];
+            x[m] = mkc<T>(sv.x * sc, sv.y * sc);
         }
-        dft_regs<T, DIR, 16>(e);
-        dft_regs<T, DIR, 16>(o);
-        // X[p] = E[p] + W32^p O[p], X[p + 16] = E[p] - W32^p O[p]
+    }
+    fs_dft<T, -1, R1>(x);
 #pragma unroll
-        for (int p = 0; p < 16; p++) {
-            const C ev = e[dft_out<16>(p)];
-            C ov = o[dft_out<16>(p)];
-            if (p) ov = cmul<T>(ov, w32<T, DIR>(p));
-            a[2 * dft_out<16>(p)] = mkc<T>(ev.x + ov.x, ev.y + ov.y);
-            a[2 * dft_out<16>(p) + 1] = mkc<T>(ev.x - ov.x, ev.y - ov.y);
+    for (int k1 = 0; k1 < R1; k1++) {
+        C v = x[fs_out<R1>(k1)];
+        if (k1) v = cmul<T>(v, tw1[j * k1]);
+        S[k1 * (R2 + 1) + j] = v;
+    }
+    __syncthreads();
+    if (!live) return;
+    C *Hrow = H + ((size_t)b * N0 + a) * n1;
+    for (int k1 = j; k1 < R1; k1 += R2) {
+        C y[R2];
+#pragma unroll
+        for (int jj = 0; jj < R2; jj++) y[jj] = S[k1 * (R2 + 1) + jj];
+        fs_dft<T, -1, R2>(y);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; k2++) Hrow[k1 + R1 * k2] = y[fs_out<R2>(k2)];
+    }
+}
+
+template <typename T, int MODE, int R1, int R2>
+__global__ void __launch_bounds__(128)
+k_rowifft_crop_fs(const cplx_t<T> *__restrict__ Hp, int N0, int N1, const T *__restrict__ c0,
+                  const T *__restrict__ c1, const cplx_t<T> *__restrict__ tw1, int plane0,
+                  CropArgs<T> ca)
+{
+    using C = cplx_t<T>;
+    constexpr int n1 = R1 * R2, RPC = 128 / R2;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double sh[32];
+    const int line = threadIdx.x / R2, j = threadIdx.x - line * R2;
+    C *S = (C *)smraw + line * fs_row_stride<R1, R2>();
+    const int b = blockIdx.y, gb = plane0 + b, a = blockIdx.x * RPC + line;
+    const bool live = a < N0;
+    const C *Hrow = Hp + ((size_t)b * N0 + (live ? a : 0)) * n1;
+    C x[R1];
+#pragma unroll
+    for (int m = 0; m < R1; m++) x[m] = live ? Hrow[j + R2 * m] : mkc<T>(0, 0);
+    fs_dft<T, +1, R1>(x);
+#pragma unroll
+    for (int k1 = 0; k1 < R1; k1++) {
+        C v = x[fs_out<R1>(k1)];
+        if (k1) {
+            C w = tw1[j * k1];
+            w.y = -w.y;
+            v = cmul<T>(v, w);
         }
+        S[k1 * (R2 + 1) + j] = v;
+    }
+    __syncthreads();
+    T s = 0;
+    if (live) {
+        const T sa = c0[a];
+        for (int k1 = j; k1 < R1; k1 += R2) {
+            C y[R2];
+#pragma unroll
+            for (int jj = 0; jj < R2; jj++) y[jj] = S[k1 * (R2 + 1) + jj];
+            fs_dft<T, +1, R2>(y);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; k2++) {
+                // output index l1 = k1 + R1 k2 is column c = l1 + N1/2 (mod n1)
+                const int c = (k1 + R1 * k2 + N1 / 2) & (n1 - 1);
+                if (c < N1) {
+                    const C g = y[fs_out<R2>(k2)];
+                    const T sc = sa * c1[c];
+                    const C z = mkc<T>(g.x * sc, g.y * sc);
+                    const size_t o = (size_t)gb * ca.out_stride + (size_t)a * N1 + c;
+                    ca.out[o] = z;
+                    if (MODE == CM_INIT) ca.p_out[o] = z;
+                    s += z.x * z.x + z.y * z.y;
+                }
+            }
+        }
+    }
+    if (MODE != CM_PLAIN) {
+        const double d = block_sum_t<T>(s, sh);
+        if (threadIdx.x == 0) ca.part[(size_t)gb * ca.part_stride + blockIdx.x] = d;
     }
 }
 
@@ -660,10 +881,14 @@ template <typename T, int DIR, int R> __device__ __forceinline__ void fs_dft(cpl
 // contiguous bytes, per step), the exchange goes through shared memory
 // (column stride padded so neither pass meets a bank twice), pass 2 writes
 // the N0 kept rows to H'.
-template <int R1, int R2> __host__ __device__ constexpr int fs_col_stride()
+
+// shared memory of k_colfft_interp_fs: four columns of n0 + 8 plus the exchange
+template <typename T> static size_t smem_colfs_of(int R1, int R2)
 {
-    // R1 x (R2 + 1) rounded up to 4 mod 16 elements
-    return ((R1 * (R2 + 1) + 11) / 16) * 16 + 4;
+    const int cs = R1 == 32 && R2 == 32   ? fs_col_stride<32, 32>()
+                   : R1 == 32 && R2 == 16 ? fs_col_stride<32, 16>()
+                                          : fs_col_stride<16, 16>();
+    return sizeof(cplx_t<T>) * 4 * ((size_t)R1 * R2 + 8 + cs);
 }
 
 template <typename T, int R1, int R2>
@@ -886,6 +1111,15 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     while (rows > 1 && 2 * sizeof(C) * fft_buf((size_t)rows * t.n1) > ((size_t)112 << 10)) rows--;
     smem_col = 2 * sizeof(C) * fft_buf((size_t)BC * n0);
     smem_row = 2 * sizeof(C) * fft_buf((size_t)rows * n1);
+    // row passes as four-step FFTs where n1 = R1 x R2 is 256, 512 or 1024:
+    // 128 / R2 rows per CTA (the CTA count also sets the crop pass's number
+    // of partial sums per plane)
+    row_fs = n1 == 1024 || n1 == 512 || n1 == 256;
+    if (row_fs) {
+        const int r1 = n1 == 256 ? 16 : 32, r2 = n1 / r1;
+        rows = 128 / r2;
+        smem_row = sizeof(C) * (size_t)rows * r1 * (r2 + 1);
+    }
     // adjoint: planes per gather pass 8 (default), 4, 2 or 1 -- the
     // autotuner's cap, else NUDIM_TUNE_PLANES
     Pa = 8;
@@ -953,6 +1187,33 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     }
     NUDIM_CUDA(cudaFuncSetAttribute(k_colifft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     lim_colifft));
+    {
+        // the four-step row passes' exchange buffers (FP64 1024 points: 68 KB)
+        const int lr1 = (int)(sizeof(C) * 4 * fs_row_stride<32, 32>());
+        const int lr2 = (int)(sizeof(C) * 8 * fs_row_stride<32, 16>());
+        const int lr3 = (int)(sizeof(C) * 8 * fs_row_stride<16, 16>());
+#define NUDIM_ROWFS_ATTR(R1, R2, L)                                                              \
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft_fs<T, PM_COMPLEX, R1, R2>,                          \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, L));           \
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft_fs<T, PM_REAL_INIT, R1, R2>,                        \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, L));           \
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_PLAIN, R1, R2>,                      \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, L));           \
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_DOT, R1, R2>,                        \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, L));           \
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_INIT, R1, R2>,                       \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, L))
+        NUDIM_ROWFS_ATTR(32, 32, lr1);
+        NUDIM_ROWFS_ATTR(32, 16, lr2);
+        NUDIM_ROWFS_ATTR(16, 16, lr3);
+#undef NUDIM_ROWFS_ATTR
+    }
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs<T, 32, 32>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs<T, 32, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs<T, 16, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
     // the four-step column IFFTs' exchange buffers (FP64 1024 points: 68 KB)
     NUDIM_CUDA(cudaFuncSetAttribute(k_colifft_fs<T, 32, 32>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1024,7 +1285,21 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
         {
             ProfScope ps(ctx, PK_PAD, st, nb * c * ((double)N0 * N1 + (double)N0 * n1));
             dim3 g(ceil_div(N0, rows), nb);
-            if (pa.mode == PM_COMPLEX)
+#define NUDIM_ROWFS(MD, R1, R2)                                                                  \
+    k_rowfft_fs<T, MD, R1, R2><<<g, 128, smem_row, st>>>(pa.src, pa.src_stride, N0, N1, c0, c1, \
+                                                          tw1, p0, H, pa.f_init, pa.f_stride)
+            if (row_fs) {
+                if (pa.mode == PM_COMPLEX) {
+                    if (n1 == 1024) NUDIM_ROWFS(PM_COMPLEX, 32, 32);
+                    else if (n1 == 512) NUDIM_ROWFS(PM_COMPLEX, 32, 16);
+                    else NUDIM_ROWFS(PM_COMPLEX, 16, 16);
+                } else {
+                    if (n1 == 1024) NUDIM_ROWFS(PM_REAL_INIT, 32, 32);
+                    else if (n1 == 512) NUDIM_ROWFS(PM_REAL_INIT, 32, 16);
+                    else NUDIM_ROWFS(PM_REAL_INIT, 16, 16);
+                }
+            } else if (pa.mode == PM_COMPLEX)
+#undef NUDIM_ROWFS
                 k_rowfft<T, PM_COMPLEX><<<g, 256, smem_row, st>>>(pa.src, pa.src_stride, N0, N1,
                                                                    n1, logn1, rows, c0, c1, tw1,
                                                                    p0, H, nullptr, 0);
@@ -1040,8 +1315,17 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
                          tab + nb * c * ((double)N0 * n1 + (double)smax * M));
             // one radix-16 butterfly per thread: 64 threads per column
             const int thr = std::min(32 * col_warps<T>(), std::max(64, 64 * BC));
-            k_colfft_interp<T><<<dim3(nblk, nb), thr, smem_col, st>>>(
-                H, N0, n0, logn0, n1, BC, tw0, blk_off, ent, e_rb, e_cc, e_qa, e_q1, nE, M, smax, P);
+#define NUDIM_COLFS(R1, R2)                                                                      \
+    k_colfft_interp_fs<T, R1, R2><<<dim3(nblk, nb), thr, smem_colfs_of<T>(R1, R2), st>>>(             \
+        H, N0, n1, tw0, blk_off, ent, e_rb, e_cc, e_qa, e_q1, nE, M, smax, P)
+            if (BC == 4 && n0 == 1024) NUDIM_COLFS(32, 32);
+            else if (BC == 4 && n0 == 512) NUDIM_COLFS(32, 16);
+            else if (BC == 4 && n0 == 256) NUDIM_COLFS(16, 16);
+            else
+                k_colfft_interp<T><<<dim3(nblk, nb), thr, smem_col, st>>>(
+                    H, N0, n0, logn0, n1, BC, tw0, blk_off, ent, e_rb, e_cc, e_qa, e_q1, nE, M,
+                    smax, P);
+#undef NUDIM_COLFS
             NUDIM_LAUNCH_CHECK();
         }
         {
@@ -1122,6 +1406,21 @@ int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropAr
         {
             ProfScope ps(ctx, PK_CROP, st, nb * c * ((double)N0 * n1 + 2.0 * N0 * N1));
             dim3 g(ceil_div(N0, rows), nb);
+#define NUDIM_CROPFS(MD, R1, R2)                                                                 \
+    k_rowifft_crop_fs<T, MD, R1, R2><<<g, 128, smem_row, st>>>(Hp, N0, N1, c0, c1, tw1, p0, ca)
+#define NUDIM_CROPFS_N(MD)                                                                       \
+    do {                                                                                        \
+        if (n1 == 1024) NUDIM_CROPFS(MD, 32, 32);                                               \
+        else if (n1 == 512) NUDIM_CROPFS(MD, 32, 16);                                           \
+        else NUDIM_CROPFS(MD, 16, 16);                                                          \
+    } while (0)
+            if (row_fs) {
+                if (ca.mode == CM_PLAIN) NUDIM_CROPFS_N(CM_PLAIN);
+                else if (ca.mode == CM_DOT) NUDIM_CROPFS_N(CM_DOT);
+                else NUDIM_CROPFS_N(CM_INIT);
+            } else
+#undef NUDIM_CROPFS_N
+#undef NUDIM_CROPFS
             switch (ca.mode) {
             case CM_PLAIN: k_rowifft_crop<T, CM_PLAIN><<<g, 256, smem_row, st>>>(Hp, N0, N1, n1, logn1, rows, c0, c1, tw1, p0, ca); break;
             case CM_DOT: k_rowifft_crop<T, CM_DOT><<<g, 256, smem_row, st>>>(Hp, N0, N1, n1, logn1, rows, c0, c1, tw1, p0, ca); break;
