@@ -11,15 +11,23 @@ SNR 0.5, reconstructed at np = nx = 384, nz = 256, padangle 1, 50 HIO + 50
 ER, anisotropic-diffusion denoise.  `value` is the mixed form (FP32
 spreading/FFT/stencils, FP64 tables), inputs resident in HBM; `e2e` is the
 same metric through the C ABI with host buffers (tilt series in, volume out,
-setup included); `fp64_plain` is the FP64 form on the same job.  Further
-legs on the same line: `batched` (48 uneven TV jobs stepped together, one
-stream each), `serving` (Poisson arrivals into the continuous-batching
-server, p50/p99 latency), `cpu_baseline` (the oracle port on the host cores,
-a bounded sample), and with --large the 768^2 x 256 TV configuration with
-its FP64 correction.
+setup included); `fp64_plain` is the FP64 form on the same job (with its own
+e2e and its roofline against the GPU's measured FP64 FMA rate).  Further
+legs on the same line: `accuracy` (the whole 50 HIO + 50 ER at 16 Z-planes in
+every form against the FP64 form, with the FP64 loop's own floors under
+1e-15, 1e-13 and FP32-sized input perturbations), `small_config` (the
+128^3, 20 ER, TV configuration: GPU time in both forms and the oracle on the
+host cores), `batched` (48 uneven TV jobs stepped together, one stream
+each), `serving` (Poisson arrivals into the continuous-batching server,
+p50/p99 latency), `cpu_baseline` (the oracle on the host cores: whole
+iterations of the workload's geometry at one Z-plane per thread, and on one
+core), and with --large the 768^2 x 256 TV configuration with its FP64
+correction.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-       [--large] [--batch-jobs J] [--serve-jobs J] [--autotune]
+       [--large] [--batch-jobs J] [--serve-jobs J] [--serve-rate R] [--serve-fp64
+       [--serve-fp64-jobs J] [--serve-fp64-rate R]] [--no-accuracy] [--no-cfg1]
+       [--autotune]
        python bench.py --tv NZxNYxNX      (the TV kernels alone)
 Under torchrun each rank runs an independent replica on its own GPU
 (the path has no cross-rank exchange): value = all ranks' voxel-iterations
@@ -486,6 +494,68 @@ def accuracy_leg(ctx, r, nz=16, snaps=(1, 2, 5, 10, 50, 75, 100)):
     return res
 
 
+def cfg1_leg(ctx, steps=5, cpu=True):
+    """The small plain-form configuration (128^3 blob phantom, 41 tilts
+    -60..60 step 3, np = 128, padangle 1, --weight, 20 ER with TV): GPU time
+    per outer iteration in both forms (CUDA events on the job's stream, after
+    2 warm-up iterations), and the oracle on the host cores -- all threads
+    on the whole volume, and one thread on 8 of its Z-planes (the per-plane
+    work dominates) -- 1 outer iteration each after setup."""
+    import copy
+
+    import nudim_gb300 as ng
+    from nudim_gb300.synth import CONFIGS, MASTER_SEED, add_noise, blob_phantom
+    from oracle import orc
+    c = CONFIGS["cfg1"]
+    r = dict(c["recon"])
+    orc.build()
+    vol = blob_phantom(seed=MASTER_SEED, **c["phantom"])
+    s = c["sim"]
+    proj = add_noise(orc.project_2d1d(vol, s["np"], s["gam_min"], s["gam_max"], s["interval"]),
+                     s["snr"], MASTER_SEED + 1)
+    V = r["nz"] * r["np"] ** 2
+    out = {"config": "128^3 blob phantom, 41 tilts -60..60 step 3, np=nx=128, nz=128, "
+                     "padangle 1, --weight, 20 ER, TV", "voxels": V}
+    for name, prec in (("fp64_plain", ng.FP64), ("mixed", ng.MIXED)):
+        job = ng.Job(ctx, **job_kwargs(r, prec))
+        job.set_projections(proj)
+        job.step(2)
+        ms = timed_steps(ctx, job, steps)
+        job.close()
+        out[name] = {"ms_per_step": ms / steps, "value": V * steps / (ms / 1e3),
+                     "unit": "voxel-iters/s"}
+    if cpu:
+        threads = os.cpu_count() or 1
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        kw = dict(nx=r["nx"], nz=r["nz"], np=r["np"], gam_min=r["gam_min"],
+                  gam_max=r["gam_max"], interval=r["interval"], padangle=r["padangle"],
+                  nhio=r["nhio"], ner=r["ner"], denoise=r["denoise"], weight=r["weight"])
+        R = orc.Recon(proj, nthreads=threads, **kw)
+        t0 = time.perf_counter()
+        R.iterate(1)
+        t_all = time.perf_counter() - t0
+        R.close()
+        sub = copy.deepcopy(c)
+        sub["phantom"]["shape"] = (8,) + tuple(sub["phantom"]["shape"][1:])
+        vol8 = blob_phantom(seed=MASTER_SEED, **sub["phantom"])
+        proj8 = orc.project_2d1d(vol8, s["np"], s["gam_min"], s["gam_max"], s["interval"])
+        R = orc.Recon(add_noise(proj8, s["snr"], MASTER_SEED + 1), nthreads=1,
+                      **dict(kw, nz=8))
+        t0 = time.perf_counter()
+        R.iterate(1)
+        t_one = time.perf_counter() - t0
+        R.close()
+        out["cpu_oracle"] = {
+            "all_cores": {"cores": threads, "s_per_iter": t_all, "value": V / t_all,
+                          "unit": "voxel-iters/s", "sample": "1 outer iteration, whole volume"},
+            "single_core": {"cores": 1, "s_per_iter_8_planes": t_one,
+                            "value": 8 * r["np"] ** 2 / t_one, "unit": "voxel-iters/s",
+                            "sample": "1 outer iteration of the geometry with 8 Z-planes"}}
+    log("cfg1: FP64 %.1f ms, mixed %.1f ms per iteration" % (out["fp64_plain"]["ms_per_step"],
+                                                            out["mixed"]["ms_per_step"]))
+    return out
+
+
 def fp64_peak():
     """The FP64 and FP32 FMA rates of this GPU (bin/fp64_peak: independent FMA
     chains, CUDA events), or None when the probe is missing."""
@@ -715,6 +785,9 @@ def run_ours(args):
     acc = None
     if not args.no_accuracy:
         acc = accuracy_leg(ctx, r, nz=args.accuracy_nz)
+    small = None
+    if not args.no_cfg1:
+        small = cfg1_leg(ctx, cpu=rank == 0 and not args.no_cpu)
 
     line = {
         "metric": "voxel-iters/s", "value": value, "unit": "voxel-iters/s", "n_gpus": ws,
@@ -752,6 +825,8 @@ def run_ours(args):
         line["mixed_over_fp64"] = value / v64
         line["rel_l2_mixed_vs_fp64_after_1_iteration"] = err1
         line["rel_l2_mixed_vs_fp64_after_warmup"] = err
+    if small is not None:
+        line["small_config"] = small
     if acc is not None:
         tot = str(r["nhio"] + r["ner"])
         rel_acc = acc["rel_l2_vs_fp64"]
@@ -775,8 +850,9 @@ def run_ours(args):
     if args.serve_jobs > 0:
         line["serving"] = {"mixed": serving_bench(ctx, args.serve_jobs, args.serve_rate, ng.MIXED)}
         if args.serve_fp64:
-            line["serving"]["fp64_plain"] = serving_bench(ctx, args.serve_jobs, args.serve_rate,
-                                                          ng.FP64)
+            line["serving"]["fp64_plain"] = serving_bench(
+                ctx, args.serve_fp64_jobs or args.serve_jobs,
+                args.serve_fp64_rate or args.serve_rate, ng.FP64)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(r)
     ctx.close()
@@ -833,6 +909,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the accuracy leg (reduced-nz 50 HIO + 50 ER in every form)")
+    ap.add_argument("--no-cfg1", action="store_true",
+                    help="skip the small-configuration leg (128^3, 20 ER, TV: GPU both forms, "
+                         "CPU oracle)")
     ap.add_argument("--accuracy-nz", type=int, default=16,
                     help="Z-planes of the accuracy leg's job (default 16)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -843,10 +922,15 @@ def main():
                     help="also run the large-volume configuration (768^2 x 256, ~3 min)")
     ap.add_argument("--batch-jobs", type=int, default=48,
                     help="jobs in the batched measurement (0: skip)")
-    ap.add_argument("--serve-jobs", type=int, default=16,
+    ap.add_argument("--serve-jobs", type=int, default=24,
                     help="jobs in the serving measurement (0: skip)")
-    ap.add_argument("--serve-rate", type=float, default=0.5, help="Poisson arrivals, jobs/s")
+    ap.add_argument("--serve-rate", type=float, default=1.0, help="Poisson arrivals, jobs/s")
     ap.add_argument("--serve-fp64", action="store_true", help="also serve the FP64 form")
+    ap.add_argument("--serve-fp64-jobs", type=int, default=0,
+                    help="jobs in the FP64 serving measurement (default: --serve-jobs)")
+    ap.add_argument("--serve-fp64-rate", type=float, default=0.0,
+                    help="Poisson arrivals of the FP64 serving measurement, jobs/s (default: "
+                         "--serve-rate; the FP64 form's capacity is far lower)")
     ap.add_argument("--nz", type=int, default=0,
                     help="override the number of Z-planes (small-case profiling only)")
     ap.add_argument("--autotune", action="store_true",

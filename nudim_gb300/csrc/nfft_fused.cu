@@ -509,6 +509,121 @@ k_colfft_interp_fs(const cplx_t<T> *__restrict__ H, int N0, int n1,
     }
 }
 
+// ================================================================ K2'' column pass, two planes
+// The FP32 trafo column pass for two Z-planes per CTA (n0 = R1 x R2, BC =
+// 4): 128 threads run each plane's four column FFTs (all 256 busy), each
+// plane's exchange goes through its own column buffer (pass 1 writes the
+// twiddled rows there, a barrier, pass 2 reads them into registers, a
+// barrier, pass 2 writes the transformed columns over them: one 4 x GS
+// buffer per plane, GS = 4 mod 16 so neither pass meets a bank twice), and
+// each thread then interpolates its (node, block) entries for both planes
+// with one read of the entry's record: the record loads -- the column
+// pass's long-latency reads -- are shared by two planes.
+template <int R1, int R2> __host__ __device__ constexpr int fs2_gs()
+{
+    // at least R1 x (R2 + 1) (the exchange) and R1 R2 (the column), 4 mod 16
+    return ((R1 * (R2 + 1) + 11) / 16) * 16 + 4;
+}
+
+template <int R1, int R2>
+__global__ void __launch_bounds__(256, 3)
+k_colfft_interp_fs2(const float2 *__restrict__ H, int N0, int n1, int nb_planes,
+                    const float2 *__restrict__ tw0, const int *__restrict__ blk_off,
+                    const int *__restrict__ ent, const int *__restrict__ e_rb,
+                    const int *__restrict__ e_cc, const float *__restrict__ e_qa,
+                    const float *__restrict__ e_q1, int nE, int M, int smax,
+                    float2 *__restrict__ part)
+{
+    using C = float2;
+    constexpr int n0 = R1 * R2, BC = 4, GS = fs2_gs<R1, R2>();
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *Gs = (C *)smraw;  // [plane 0..1][column][GS]
+    const int cb = blockIdx.x, pb = blockIdx.y * 2;
+    const bool two = pb + 1 < nb_planes;
+    const int pp = threadIdx.x >> 7, t = threadIdx.x & 127;
+    const int lane = t & 31, warp = t >> 5;
+    const int c = lane & 3, j = warp * 8 + (lane >> 2);
+    const bool fft = t < 4 * R2 && (pp == 0 || two);
+    C *Gp = Gs + (size_t)pp * BC * GS;
+    C y[R2];
+    if (fft) {
+        const C *Hb = H + (size_t)(pb + pp) * N0 * n1 + (size_t)cb * BC + c;
+        C x[R1];
+#pragma unroll
+        for (int m = 0; m < R1; m++) {
+            const int l0 = j + R2 * m;
+            const int a = (l0 < n0 / 2 ? l0 : l0 - n0) + N0 / 2;
+            x[m] = (a >= 0 && a < N0) ? Hb[(size_t)a * n1] : make_float2(0.f, 0.f);
+        }
+        fs_dft<float, -1, R1>(x);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) {
+            C v = x[fs_out<R1>(k1)];
+            if (k1) v = cmul<float>(v, tw0[j * k1]);
+            Gp[c * GS + k1 * (R2 + 1) + j] = v;
+        }
+    }
+    __syncthreads();
+    // pass 2 (R1 / R2 columns of the exchange per thread; R1 == R2 here or
+    // R1 = 2 R2): read them all before any thread overwrites the buffer
+    constexpr int NK = R1 / R2;
+    C yy[NK][R2];
+    if (fft) {
+#pragma unroll
+        for (int q = 0; q < NK; q++) {
+            const int k1 = j + q * R2;
+#pragma unroll
+            for (int jj = 0; jj < R2; jj++) yy[q][jj] = Gp[c * GS + k1 * (R2 + 1) + jj];
+        }
+    }
+    __syncthreads();
+    if (fft) {
+#pragma unroll
+        for (int q = 0; q < NK; q++) {
+            const int k1 = j + q * R2;
+#pragma unroll
+            for (int jj = 0; jj < R2; jj++) y[jj] = yy[q][jj];
+            fs_dft<float, -1, R2>(y);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; k2++) Gp[c * GS + k1 + R1 * k2] = y[fs_out<R2>(k2)];
+        }
+    }
+    __syncthreads();
+    const int beg = blk_off[cb], end = blk_off[cb + 1];
+    const int m0 = n0 - 1;
+    for (int e = beg + threadIdx.x; e < end; e += blockDim.x) {
+        const int js = ent[e], rb = e_rb[e], ccn = e_cc[e];
+        const int cl0 = ccn & 255, cnt = ccn >> 8;
+        float qa[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) qa[i] = e_qa[(size_t)i * nE + e];
+        float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
+        for (int q = 0; q < cnt; q++) {
+            const int col = (cl0 + q) & (BC - 1);
+            const C *g0 = Gs + (size_t)col * GS, *g1 = g0 + BC * GS;
+            float2 s0 = make_float2(0.f, 0.f), s1 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int r = (rb + 2 * i) & m0;
+                const float4 p0 = *(const float4 *)(g0 + r);
+                const float4 p1 = *(const float4 *)(g1 + r);
+                const float2 qa0 = make_float2(qa[2 * i], qa[2 * i]);
+                const float2 qa1 = make_float2(qa[2 * i + 1], qa[2 * i + 1]);
+                s0 = __ffma2_rn(qa0, make_float2(p0.x, p0.y), s0);
+                s0 = __ffma2_rn(qa1, make_float2(p0.z, p0.w), s0);
+                s1 = __ffma2_rn(qa0, make_float2(p1.x, p1.y), s1);
+                s1 = __ffma2_rn(qa1, make_float2(p1.z, p1.w), s1);
+            }
+            const float w = e_q1[(size_t)q * nE + e];
+            const float2 ww = make_float2(w, w);
+            acc0 = __ffma2_rn(ww, s0, acc0);
+            acc1 = __ffma2_rn(ww, s1, acc1);
+        }
+        part[((size_t)pb * smax + (js & 7)) * M + (js >> 3)] = acc0;
+        if (two) part[((size_t)(pb + 1) * smax + (js & 7)) * M + (js >> 3)] = acc1;
+    }
+}
+
 // ================================================================ K3 combine + epilogue
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256)
@@ -1208,6 +1323,12 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
         NUDIM_ROWFS_ATTR(16, 16, lr3);
 #undef NUDIM_ROWFS_ATTR
     }
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs2<32, 32>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs2<32, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs2<16, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
     NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs<T, 32, 32>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
     NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs<T, 32, 16>,
@@ -1318,7 +1439,15 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
 #define NUDIM_COLFS(R1, R2)                                                                      \
     k_colfft_interp_fs<T, R1, R2><<<dim3(nblk, nb), thr, smem_colfs_of<T>(R1, R2), st>>>(             \
         H, N0, n1, tw0, blk_off, ent, e_rb, e_cc, e_qa, e_q1, nE, M, smax, P)
-            if (BC == 4 && n0 == 1024) NUDIM_COLFS(32, 32);
+#define NUDIM_COLFS2(R1, R2)                                                                     \
+    k_colfft_interp_fs2<R1, R2><<<dim3(nblk, ceil_div(nb, 2)), 256,                             \
+                                  sizeof(float2) * 2 * 4 * fs2_gs<R1, R2>(), st>>>(             \
+        (const float2 *)H, N0, n1, nb, (const float2 *)tw0, blk_off, ent, e_rb, e_cc,            \
+        (const float *)e_qa, (const float *)e_q1, nE, M, smax, (float2 *)P)
+            if (sizeof(T) == 4 && BC == 4 && n0 == 1024) NUDIM_COLFS2(32, 32);
+            else if (sizeof(T) == 4 && BC == 4 && n0 == 512) NUDIM_COLFS2(32, 16);
+            else if (sizeof(T) == 4 && BC == 4 && n0 == 256) NUDIM_COLFS2(16, 16);
+            else if (BC == 4 && n0 == 1024) NUDIM_COLFS(32, 32);
             else if (BC == 4 && n0 == 512) NUDIM_COLFS(32, 16);
             else if (BC == 4 && n0 == 256) NUDIM_COLFS(16, 16);
             else
@@ -1326,6 +1455,7 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
                     H, N0, n0, logn0, n1, BC, tw0, blk_off, ent, e_rb, e_cc, e_qa, e_q1, nE, M,
                     smax, P);
 #undef NUDIM_COLFS
+#undef NUDIM_COLFS2
             NUDIM_LAUNCH_CHECK();
         }
         {

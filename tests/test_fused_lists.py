@@ -3,7 +3,8 @@ build_fused_lists) on the CPU: every node's trafo entries (per column block)
 and adjoint tile entries (per R x BCa tile) must reproduce exactly its window
 weights psi0[r - u0] * psi1[c - u1] on its 14 x 14 window of the oversampled
 grid (wrapping at the edges), each grid point once; tile lists are in
-ascending node order and each block's tiles ordered longest first.  The grid
+ascending node order, every tile listed once, longest list first; a
+node's trafo entries share its first row and row weights.  The grid
 path's spreading tile lists (build_tile_lists) hold, per tile, exactly the
 nodes whose window meets it, ascending.  A g++ harness links tables.cpp
 directly (no GPU)."""
@@ -69,6 +70,19 @@ static int check(int N, int M, int BC, bool pair_rows, unsigned seed)
                 }
             }
         }
+    // the first row and the 16 row weights depend on the node only
+    {
+        std::vector<int> first(M, -1);
+        for (size_t e = 0; e < nE; e++) {
+            int j = L.ent[e] / 8;
+            if (first[j] < 0) { first[j] = (int)e; continue; }
+            size_t f = (size_t)first[j];
+            if (L.ent_rb[e] != L.ent_rb[f]) return 32;
+            for (int i = 0; i < 16; i++)
+                if (L.ent_qa.data()[(size_t)i * nE + e] != L.ent_qa.data()[(size_t)i * nE + f])
+                    return 33;
+        }
+    }
     for (int j = 0; j < M; j++) {
         if ((int)slots[j].size() != L.nslots[j] || L.nslots[j] > L.smax) return 30;
         std::vector<int> seen(8, 0);
