@@ -212,14 +212,14 @@ def timed_steps(ctx, job, steps, nvtx=None):
 # DRAM bytes per Z-plane of the adjoint NFFT's three kernels, from ncu captures
 # of 32-plane launches on the same geometry: dram__bytes_read.sum +
 # dram__bytes_write.sum / 32.
-MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((163.802880e6 + 218.726656e6)    # k_spread_gather
-                                      + (256.0e6 + 96.0e6)             # k_colifft (model)
+MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((172.924160e6 + 216.713216e6)    # k_spread_gather
+                                      + (268.486656e6 + 75.897088e6)   # k_colifft_fs
                                       + (100.737792e6 + 36.037120e6)) / 32  # k_rowifft_crop
 
 
 def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):
     """Roofline of the dominant kernel group, the adjoint NFFT (k_spread_gather
-    + k_colifft + k_rowifft_crop).  Its unit is one Z-plane's adjoint NFFT,
+    + k_spread_fixup + k_colifft_fs + k_rowifft_crop_fs).  Its unit is one Z-plane's adjoint NFFT,
     whose algorithmic bytes are those of the unfused NFFT: c (P^2 + 4 n^2 + M)
     -- coefficients, the n x n oversampled grid written, transformed (read +
     write) and read back, and the node values.  achieved = units x that / the
@@ -240,7 +240,8 @@ def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):
     achieved = units * unit / secs / 1e9
     return "adjoint NFFT", {
         "bound": "hbm",
-        "kernel": "adjoint NFFT (k_spread_gather + k_colifft + k_rowifft_crop)",
+        "kernel": "adjoint NFFT (k_spread_gather + k_spread_fixup + k_colifft_fs + "
+                  "k_rowifft_crop_fs)",
         "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
         "frac": round(achieved / peak_gbs, 4),
         "traffic": round(MEASURED_ADJOINT_TRAFFIC_PER_PLANE * planes_per_launch),

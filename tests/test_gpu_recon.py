@@ -221,3 +221,33 @@ def test_consecutive_fp64_iterations_stay_fp64(gpu_ctx, orc, nudim_built):
     vc, rhc, _ = run_gpu(gpu_ctx, nudim_built, proj, precision=1, correct_every=1, **kw)
     assert rel(vc, v64) < 1e-4
     assert np.allclose(rhc, rh64, rtol=1e-4)
+
+
+def test_mixed_form_within_the_fp32_sized_floor(gpu_ctx, nudim_built):
+    """The mid-size workload's geometry (384^2 planes, 61 tilts -60..60 step
+    2, --weight, diffusion) at 16 Z-planes over the whole 50 HIO + 50 ER.
+    HIO's sign test turns any FP32-sized difference into flipped voxels, so
+    the attainable bar for a form that rounds in FP32 is the FP64 loop's own
+    distance under an FP32-sized (6e-8 relative) perturbation of its tilt
+    series: the mixed form must stay within 3x of it, and an FP64-sized
+    (1e-13) perturbation must stay far below it (the FP64 loop itself is
+    not chaotic at that size)."""
+    import copy
+
+    from nudim_gb300.synth import CONFIGS, MASTER_SEED, make_inputs
+    c = copy.deepcopy(CONFIGS["cfg2"])
+    nz = 16
+    c["phantom"]["shape"] = (nz,) + tuple(c["phantom"]["shape"][1:])
+    r = dict(c["recon"], nz=nz)
+    _, proj = make_inputs(gpu_ctx, None, seed=MASTER_SEED, cfg=c)
+    kw = {k: r[k] for k in ("nx", "nz", "np", "gam_min", "gam_max", "interval", "padangle",
+                            "nhio", "ner", "denoise", "weight")}
+    ref, _, _ = run_gpu(gpu_ctx, nudim_built, proj, **kw)
+    noise = np.random.default_rng(1).standard_normal(proj.shape)
+    p32, _, _ = run_gpu(gpu_ctx, nudim_built, proj * (1 + 6e-8 * noise), **kw)
+    p64, _, _ = run_gpu(gpu_ctx, nudim_built, proj * (1 + 1e-13 * noise), **kw)
+    mixed, _, _ = run_gpu(gpu_ctx, nudim_built, proj, precision=1, **kw)
+    floor32, floor64, err = rel(p32, ref), rel(p64, ref), rel(mixed, ref)
+    print("mixed %.3e, FP32-sized floor %.3e, FP64-sized floor %.3e" % (err, floor32, floor64))
+    assert floor64 < 1e-6 * floor32
+    assert err <= 3 * floor32
