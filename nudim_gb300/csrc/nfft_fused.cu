@@ -624,6 +624,101 @@ k_colfft_interp_fs2(const float2 *__restrict__ H, int N0, int n1, int nb_planes,
     }
 }
 
+// ================================================================ K2 column pass, 8-column blocks
+// The FP32 trafo column pass on blocks of 8 columns (n0 = R1 x R2): a
+// node's 14 window columns meet 2 or 3 blocks instead of 4 or 5, so there
+// are fewer (node, block) entries -- fewer record loads and partial sums --
+// and more columns per entry.  256 threads run the 8 column FFTs (a warp
+// reads 4 rows x 8 columns per step), the column buffer (stride GS = 2 mod
+// 16) doubles as the exchange; then the interpolation as in
+// k_colfft_interp.
+template <int R1, int R2> __host__ __device__ constexpr int fs8_gs()
+{
+    return ((R1 * (R2 + 1) + 13) / 16) * 16 + 2;
+}
+
+template <int R1, int R2>
+__global__ void __launch_bounds__(256, 3)
+k_colfft_interp_fs8(const float2 *__restrict__ H, int N0, int n1,
+                    const float2 *__restrict__ tw0, const int *__restrict__ blk_off,
+                    const int *__restrict__ ent, const int *__restrict__ e_rb,
+                    const int *__restrict__ e_cc, const float *__restrict__ e_qa,
+                    const float *__restrict__ e_q1, int nE, int M, int smax,
+                    float2 *__restrict__ part)
+{
+    using C = float2;
+    constexpr int n0 = R1 * R2, BC = 8, GS = fs8_gs<R1, R2>();
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *Gs = (C *)smraw;  // [column][GS]
+    const int cb = blockIdx.x, b = blockIdx.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = lane & 7, j = warp * 4 + (lane >> 3);
+    const bool fft = j < R2;
+    if (fft) {
+        const C *Hb = H + (size_t)b * N0 * n1 + (size_t)cb * BC + c;
+        C x[R1];
+#pragma unroll
+        for (int m = 0; m < R1; m++) {
+            const int l0 = j + R2 * m;
+            const int a = (l0 < n0 / 2 ? l0 : l0 - n0) + N0 / 2;
+            x[m] = (a >= 0 && a < N0) ? Hb[(size_t)a * n1] : make_float2(0.f, 0.f);
+        }
+        fs_dft<float, -1, R1>(x);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) {
+            C v = x[fs_out<R1>(k1)];
+            if (k1) v = cmul<float>(v, tw0[j * k1]);
+            Gs[c * GS + k1 * (R2 + 1) + j] = v;
+        }
+    }
+    __syncthreads();
+    constexpr int NK = R1 / R2;
+    C yy[NK][R2];
+    if (fft) {
+#pragma unroll
+        for (int q = 0; q < NK; q++) {
+            const int k1 = j + q * R2;
+#pragma unroll
+            for (int jj = 0; jj < R2; jj++) yy[q][jj] = Gs[c * GS + k1 * (R2 + 1) + jj];
+        }
+    }
+    __syncthreads();
+    if (fft) {
+#pragma unroll
+        for (int q = 0; q < NK; q++) {
+            const int k1 = j + q * R2;
+            fs_dft<float, -1, R2>(yy[q]);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; k2++) Gs[c * GS + k1 + R1 * k2] = yy[q][fs_out<R2>(k2)];
+        }
+    }
+    __syncthreads();
+    const int beg = blk_off[cb], end = blk_off[cb + 1];
+    const int m0 = n0 - 1;
+    for (int e = beg + threadIdx.x; e < end; e += blockDim.x) {
+        const int js = ent[e], rb = e_rb[e], ccn = e_cc[e];
+        const int cl0 = ccn & 255, cnt = ccn >> 8;
+        float qa[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) qa[i] = e_qa[(size_t)i * nE + e];
+        float2 acc = make_float2(0.f, 0.f);
+        for (int q = 0; q < cnt; q++) {
+            const C *gp = Gs + (size_t)((cl0 + q) & (BC - 1)) * GS;
+            float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const float4 pr = *(const float4 *)(gp + ((rb + 2 * i) & m0));
+                s2 = __ffma2_rn(make_float2(qa[2 * i], qa[2 * i]), make_float2(pr.x, pr.y), s2);
+                s2 = __ffma2_rn(make_float2(qa[2 * i + 1], qa[2 * i + 1]), make_float2(pr.z, pr.w),
+                                s2);
+            }
+            const float w = e_q1[(size_t)q * nE + e];
+            acc = __ffma2_rn(make_float2(w, w), s2, acc);
+        }
+        part[((size_t)b * smax + (js & 7)) * M + (js >> 3)] = acc;
+    }
+}
+
 // ================================================================ K3 combine + epilogue
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256)
@@ -1169,6 +1264,8 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     // 4 columns (measured: two 4-column CTAs per SM beat one 8-column CTA)
     int bc = (int)((128 << 10) / (2 * sizeof(C) * (size_t)t.n0));
     if (bc > 4) bc = 4;
+    // the FP32 four-step column pass takes 8-column blocks (fewer entries)
+    if (sizeof(T) == 4 && (t.n0 == 1024 || t.n0 == 512 || t.n0 == 256) && t.n1 >= 64) bc = 8;
     if (bc > t.n1) bc = t.n1;
     // the autotuner's cap, else NUDIM_TUNE_BC (a tuning knob: narrower blocks
     // fit more CTAs per SM at the cost of more (node, block) entries)
@@ -1323,6 +1420,12 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
         NUDIM_ROWFS_ATTR(16, 16, lr3);
 #undef NUDIM_ROWFS_ATTR
     }
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs8<32, 32>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs8<32, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs8<16, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
     NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs2<32, 32>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
     NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs2<32, 16>,
@@ -1444,7 +1547,15 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
                                   sizeof(float2) * 2 * 4 * fs2_gs<R1, R2>(), st>>>(             \
         (const float2 *)H, N0, n1, nb, (const float2 *)tw0, blk_off, ent, e_rb, e_cc,            \
         (const float *)e_qa, (const float *)e_q1, nE, M, smax, (float2 *)P)
-            if (sizeof(T) == 4 && BC == 4 && n0 == 1024) NUDIM_COLFS2(32, 32);
+#define NUDIM_COLFS8(R1, R2)                                                                     \
+    k_colfft_interp_fs8<R1, R2><<<dim3(nblk, nb), 256, sizeof(float2) * 8 * fs8_gs<R1, R2>(),    \
+                                  st>>>((const float2 *)H, N0, n1, (const float2 *)tw0, blk_off, \
+                                        ent, e_rb, e_cc, (const float *)e_qa,                   \
+                                        (const float *)e_q1, nE, M, smax, (float2 *)P)
+            if (sizeof(T) == 4 && BC == 8 && n0 == 1024) NUDIM_COLFS8(32, 32);
+            else if (sizeof(T) == 4 && BC == 8 && n0 == 512) NUDIM_COLFS8(32, 16);
+            else if (sizeof(T) == 4 && BC == 8 && n0 == 256) NUDIM_COLFS8(16, 16);
+            else if (sizeof(T) == 4 && BC == 4 && n0 == 1024) NUDIM_COLFS2(32, 32);
             else if (sizeof(T) == 4 && BC == 4 && n0 == 512) NUDIM_COLFS2(32, 16);
             else if (sizeof(T) == 4 && BC == 4 && n0 == 256) NUDIM_COLFS2(16, 16);
             else if (BC == 4 && n0 == 1024) NUDIM_COLFS(32, 32);
@@ -1456,6 +1567,7 @@ int NfftDev<T>::trafo_fused(int nplanes, const PadArgs<T> &pa, const InterpArgs<
                     smax, P);
 #undef NUDIM_COLFS
 #undef NUDIM_COLFS2
+#undef NUDIM_COLFS8
             NUDIM_LAUNCH_CHECK();
         }
         {
@@ -1595,7 +1707,7 @@ template <typename T> int NfftDev<T>::autotune(const NfftTables &t, cudaStream_t
     float best = 0.f;
     int choice_bc = 0, choice_p = 0;
     std::vector<std::pair<int, int>> built;  // (BC, Pa) of the plans already timed
-    for (int bcc : {4, 2})
+    for (int bcc : {8, 4, 2})
         for (int pc : {8, 4, 2}) {
             if (rc) break;
             NfftDev<T> trial;

@@ -91,7 +91,7 @@ def test_autotune_chooses_a_candidate_with_the_same_results(nudim_built, orc, pr
     tuning = []
     f, g = run(nudim_built, orc, {}, 96, prec, flags=nudim_built.CTX_AUTOTUNE, tuning=tuning)
     bc, planes = tuning[0]
-    assert bc in (2, 4) and planes in (1, 2, 4, 8)
+    assert bc in (2, 4, 8) and planes in (1, 2, 4, 8)
     assert tuning[1] == tuning[0]
     assert np.array_equal(g, base[1])
     assert rel(f, base[0]) < (1e-14 if prec == 0 else 1e-6)
