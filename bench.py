@@ -925,7 +925,9 @@ def main():
                     help="jobs in the batched measurement (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=24,
                     help="jobs in the serving measurement (0: skip)")
-    ap.add_argument("--serve-rate", type=float, default=1.0, help="Poisson arrivals, jobs/s")
+    ap.add_argument("--serve-rate", type=float, default=0.4,
+                    help="Poisson arrivals, jobs/s (default below the measured capacity of "
+                         "about 0.47 jobs/s for this job mix)")
     ap.add_argument("--serve-fp64", action="store_true", help="also serve the FP64 form")
     ap.add_argument("--serve-fp64-jobs", type=int, default=0,
                     help="jobs in the FP64 serving measurement (default: --serve-jobs)")

@@ -381,7 +381,7 @@ k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int 
     const int m0 = n0 - 1;
     for (int e = beg + threadIdx.x; e < end; e += blockDim.x) {
         const int js = ent[e], rb = e_rb[e], ccn = e_cc[e];
-        const int cl0 = ccn & 255, cnt = ccn >> 8;
+        const int cl0 = ccn & 255, cnt = (ccn >> 8) & 255;
         T qa[16];
 #pragma unroll
         for (int i = 0; i < 16; i++) qa[i] = e_qa[(size_t)i * nE + e];
@@ -402,11 +402,15 @@ k_colfft_interp(const cplx_t<T> *__restrict__ H, int N0, int n0, int logn0, int 
                 sr = s2.x;
                 si = s2.y;
             } else {
+                // FP64: the window's 14 rows only (the 16-row pairs are an
+                // FP32 load shape; every FMA counts on the FP64 pipe)
+                const int odd = ccn >> 16;
 #pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    C g = gp[(rb + i) & m0];
-                    sr += qa[i] * g.x;
-                    si += qa[i] * g.y;
+                for (int i = 0; i < 14; i++) {
+                    const T w = odd ? qa[i + 1] : qa[i];
+                    C g = gp[(rb + odd + i) & m0];
+                    sr += w * g.x;
+                    si += w * g.y;
                 }
             }
             T w = e_q1[(size_t)q * nE + e];
@@ -474,7 +478,7 @@ k_colfft_interp_fs(const cplx_t<T> *__restrict__ H, int N0, int n1,
     const int m0 = n0 - 1;
     for (int e = beg + threadIdx.x; e < end; e += blockDim.x) {
         const int js = ent[e], rb = e_rb[e], ccn = e_cc[e];
-        const int cl0 = ccn & 255, cnt = ccn >> 8;
+        const int cl0 = ccn & 255, cnt = (ccn >> 8) & 255;
         T qa[16];
 #pragma unroll
         for (int i = 0; i < 16; i++) qa[i] = e_qa[(size_t)i * nE + e];
@@ -494,11 +498,15 @@ k_colfft_interp_fs(const cplx_t<T> *__restrict__ H, int N0, int n1,
                 sr = s2.x;
                 si = s2.y;
             } else {
+                // FP64: the window's 14 rows only (the 16-row pairs are an
+                // FP32 load shape; every FMA counts on the FP64 pipe)
+                const int odd = ccn >> 16;
 #pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    C g = gp[(rb + i) & m0];
-                    sr += qa[i] * g.x;
-                    si += qa[i] * g.y;
+                for (int i = 0; i < 14; i++) {
+                    const T w = odd ? qa[i + 1] : qa[i];
+                    C g = gp[(rb + odd + i) & m0];
+                    sr += w * g.x;
+                    si += w * g.y;
                 }
             }
             T w = e_q1[(size_t)q * nE + e];
@@ -593,7 +601,7 @@ k_colfft_interp_fs2(const float2 *__restrict__ H, int N0, int n1, int nb_planes,
     const int m0 = n0 - 1;
     for (int e = beg + threadIdx.x; e < end; e += blockDim.x) {
         const int js = ent[e], rb = e_rb[e], ccn = e_cc[e];
-        const int cl0 = ccn & 255, cnt = ccn >> 8;
+        const int cl0 = ccn & 255, cnt = (ccn >> 8) & 255;
         float qa[16];
 #pragma unroll
         for (int i = 0; i < 16; i++) qa[i] = e_qa[(size_t)i * nE + e];
@@ -697,7 +705,7 @@ k_colfft_interp_fs8(const float2 *__restrict__ H, int N0, int n1,
     const int m0 = n0 - 1;
     for (int e = beg + threadIdx.x; e < end; e += blockDim.x) {
         const int js = ent[e], rb = e_rb[e], ccn = e_cc[e];
-        const int cl0 = ccn & 255, cnt = ccn >> 8;
+        const int cl0 = ccn & 255, cnt = (ccn >> 8) & 255;
         float qa[16];
 #pragma unroll
         for (int i = 0; i < 16; i++) qa[i] = e_qa[(size_t)i * nE + e];
@@ -778,6 +786,31 @@ k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ 
     }
 }
 
+// Kahan-compensated sum of complex FP32 values with paired instructions:
+// y = v - c, t = s + y, c = (t - s) - y, s = t (the subtractions as fused
+// multiply-adds by -1, exact before their single rounding); the total is
+// s - c.
+struct Kahan2 {
+    float2 s, c;
+    __device__ __forceinline__ void init()
+    {
+        s = make_float2(0.f, 0.f);
+        c = make_float2(0.f, 0.f);
+    }
+    __device__ __forceinline__ void add(float2 v)
+    {
+        const float2 m1 = make_float2(-1.f, -1.f);
+        const float2 y = __ffma2_rn(m1, c, v);
+        const float2 t = __fadd2_rn(s, y);
+        c = __ffma2_rn(m1, y, __ffma2_rn(m1, s, t));
+        s = t;
+    }
+    __device__ __forceinline__ float2 value() const
+    {
+        return __ffma2_rn(make_float2(-1.f, -1.f), c, s);
+    }
+};
+
 // ================================================================ K4a spreading gather
 // The adjoint's spreading as a gather into the oversampled grid G of a chunk
 // of planes.  The grid is cut into tiles of R = 32 / BC rows x BC columns
@@ -788,8 +821,8 @@ k_combine(const cplx_t<T> *__restrict__ part, const unsigned char *__restrict__ 
 // stages entry l's weights and its node's P (weighted) values in the warp's
 // shared-memory stage, then every lane sums, for its grid point and each
 // plane, q0(row) q1(col) f over the chunk -- one paired FMA per plane and
-// entry in FP32.  FP32: plain sums within a chunk, Neumaier-compensated
-// across chunks; FP64: fused multiply-adds in ascending node order.  The tile's 32 points of each plane are one
+// entry in FP32.  FP32: plain sums within a chunk, Kahan-compensated across
+// chunks; FP64: fused multiply-adds in ascending node order.  The tile's 32 points of each plane are one
 // contiguous 256-byte (FP32) store: G is laid out column block by column
 // block, [plane][block][row][column in block], which is also the order the
 // column IFFT reads.  The work units are ranges of at most kGatherMaxEntries
@@ -813,7 +846,7 @@ template <typename T, int P> __host__ __device__ constexpr size_t gather_stage_b
 }
 
 template <typename T, bool WEIGHTED, int P>
-__global__ void __launch_bounds__(32 * kGatherWarps)
+__global__ void __launch_bounds__(32 * kGatherWarps, 3)
 k_spread_gather(SpreadArgs<T> sa, const int4 *__restrict__ units, int nunits,
                 const int *__restrict__ band_node, const T *__restrict__ band_w, int nbands,
                 int n0, int n1, int BC, int nb_planes, int plane0, cplx_t<T> *__restrict__ G,
@@ -839,12 +872,11 @@ k_spread_gather(SpreadArgs<T> sa, const int4 *__restrict__ units, int nunits,
         const int4 un = units[it];  // tile, first entry, end, partial slot (0: G)
         const int tile = un.x, beg = un.y, end = un.z;
         T ar[P], ai[P];
-        Comp<T> kr[P], ki[P];
+        Kahan2 ks[P];  // FP32: compensated totals of the chunk sums (re, im)
 #pragma unroll
         for (int p = 0; p < P; p++) {
             ar[p] = ai[p] = T(0);
-            kr[p].init();
-            ki[p].init();
+            ks[p].init();
         }
         for (int base = beg; base < end; base += 32) {
             const int n = min(32, end - base);
@@ -890,10 +922,7 @@ k_spread_gather(SpreadArgs<T> sa, const int4 *__restrict__ units, int nunits,
                     }
                 }
 #pragma unroll
-                for (int p = 0; p < P; p++) {
-                    kr[p].add(bs[p].x);
-                    ki[p].add(bs[p].y);
-                }
+                for (int p = 0; p < P; p++) ks[p].add(bs[p]);
             } else {
                 // FP64: the point's weight once per entry, then one fused
                 // multiply-add per plane and component (the FP64 pipe is
@@ -915,8 +944,9 @@ k_spread_gather(SpreadArgs<T> sa, const int4 *__restrict__ units, int nunits,
         for (int p = 0; p < P; p++) {
             if (p < np) {
                 if (sizeof(T) == 4) {
-                    ar[p] = kr[p].value();
-                    ai[p] = ki[p].value();
+                    const float2 v = ks[p].value();
+                    ar[p] = (T)v.x;
+                    ai[p] = (T)v.y;
                 }
                 const C val = mkc<T>(ar[p], ai[p]);
                 if (un.w == 0)

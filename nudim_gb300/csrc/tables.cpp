@@ -364,7 +364,7 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
             const double *ps = &t.psi[(size_t)j * 2 * kWin];
             int odd = ux & 1;
             L->ent_rb[e] = ux - odd;
-            L->ent_cc[e] = cl0 | (cnt << 8);
+            L->ent_cc[e] = cl0 | (cnt << 8) | (odd << 16);
             for (int i = 0; i < 16; i++) {
                 int t0 = i - odd;
                 qa[(size_t)i * nE + e] = (Wt)(t0 >= 0 && t0 < kWin ? ps[t0] : 0.0);

@@ -57,7 +57,8 @@ template <typename W> struct FusedLists {
     std::vector<int> blk_off, ent;          // ent = node * 8 + slot
     std::vector<unsigned char> nslots;      // blocks per node
     // per trafo entry (structure of arrays over the entries): even first
-    // window row, cl0 | cnt << 8, 16 aligned row weights, nq column weights
+    // window row, cl0 | cnt << 8 | odd << 16 (odd: the window's first row is
+    // rb + 1), 16 aligned row weights, nq column weights
     int nq = 0;
     std::vector<int> ent_rb, ent_cc;
     HostArray<W> ent_qa, ent_q1;

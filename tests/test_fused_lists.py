@@ -58,7 +58,11 @@ static int check(int N, int M, int BC, bool pair_rows, unsigned seed)
         for (int e = L.blk_off[b]; e < L.blk_off[b + 1]; e++) {
             int j = L.ent[e] / 8, slot = L.ent[e] % 8;
             slots[j].push_back(slot);
-            int rb = L.ent_rb[e], cl0 = L.ent_cc[e] & 255, cnt = L.ent_cc[e] >> 8;
+            int rb = L.ent_rb[e], cl0 = L.ent_cc[e] & 255, cnt = (L.ent_cc[e] >> 8) & 255;
+            // the parity bit names the window's first row: its weight at rb
+            // is zero when the window starts at rb + 1
+            int odd = L.ent_cc[e] >> 16;
+            if (odd != (t.u0[j] & 1)) return 34;
             for (int q = 0; q < cnt; q++) {
                 int c = b * L.BC + ((cl0 + q) & (L.BC - 1));
                 double wc = (double)L.ent_q1.data()[(size_t)q * nE + e];
