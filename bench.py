@@ -2,8 +2,10 @@
 
 Metric: voxel-iterations per second = nz * np^2 * (outer HIO/ER iterations)
 / wall time of the iteration loop (one "step" = one outer iteration of the
-whole volume: Z-FFT, 12 NFFT + 11 adjoint NFFT per Z-plane inside the
-constraint + 10-step CGNR, inverse Z-FFT, denoise, HIO/ER).
+whole volume: Z-FFT, per Z-plane the constraint's NFFT and the 10-step
+CGNR -- in the FP64 form a trafo and an adjoint NFFT per step as in the
+reference, in the mixed form one adjoint NFFT and 11 passes of the normal
+operator by Toeplitz embedding -- inverse Z-FFT, denoise, HIO/ER).
 
 Workload (default): the precision-form configuration, a 256^3 blob + shell
 phantom simulated to 61 tilts (-60..60 deg step 2) of 384 x 256 pixels at
@@ -215,39 +217,60 @@ def timed_steps(ctx, job, steps, nvtx=None):
 MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((172.924160e6 + 216.713216e6)    # k_spread_gather
                                       + (268.486656e6 + 75.897088e6)   # k_colifft_fs
                                       + (100.737792e6 + 36.037120e6)) / 32  # k_rowifft_crop
+# The same for the Toeplitz operator pass (k_rowfft_fs + k_col_toeplitz +
+# k_rowifft_crop_fs in its p^H q mode), None until captured.
+MEASURED_TOEPLITZ_TRAFFIC_PER_PLANE = None
 
 
 def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):
-    """Roofline of the dominant kernel group, the adjoint NFFT (k_spread_gather
-    + k_spread_fixup + k_colifft_fs + k_rowifft_crop_fs).  Its unit is one Z-plane's adjoint NFFT,
-    whose algorithmic bytes are those of the unfused NFFT: c (P^2 + 4 n^2 + M)
-    -- coefficients, the n x n oversampled grid written, transformed (read +
-    write) and read back, and the node values.  achieved = units x that / the
-    kernels' measured time."""
+    """Roofline of the dominant kernel group of the mixed form's iteration.
+
+    - The Toeplitz operator pass of the CGNR (k_rowfft_fs + k_col_toeplitz +
+      k_rowifft_crop_fs, class "toeplitz"): 11 per Z-plane and outer
+      iteration (one before the loop, one per step).  Unit: one Z-plane's
+      pass, c (3 P^2 + 4 P n) bytes -- p in, T p out and p read again for
+      p^H T p, and the P x n row spectra written, read and written by the
+      column pass, and read back.
+    - The adjoint NFFT (k_spread_gather + k_spread_fixup + k_colifft_fs +
+      k_rowifft_crop_fs, classes "spread" + "crop"): 11 per Z-plane and outer
+      iteration with the NFFT form of the CGNR, 1 with the Toeplitz form.
+      Unit: c (P^2 + 4 n^2 + M) -- coefficients, the n x n oversampled grid
+      written, transformed (read + write) and read back, and the node values.
+    achieved = units x unit bytes / the group's measured time."""
     total = sum(v[0] for v in prof.values())
     shares = {k: round(v[0] / total, 4) for k, v in prof.items() if v[1] > 0}
     P, nz = r["np"], r["nz"]
     n = 2 * (1 << (P - 1).bit_length())
     M = 181 * P
-    unit = csize * (P * P + 4 * n * n + M)
+    toep = prof.get("toeplitz", (0.0, 0, 0.0))
+    groups = []
+    if toep[1] > 0:
+        units = 11 * nz * steps
+        launches = toep[1] / 3.0  # three passes per launch of the group
+        unit = csize * (3 * P * P + 4 * P * n)
+        tr = MEASURED_TOEPLITZ_TRAFFIC_PER_PLANE
+        groups.append(("Toeplitz operator pass",
+                       "Toeplitz operator pass (k_rowfft_fs + k_col_toeplitz + k_rowifft_crop_fs)",
+                       toep[0], units, launches, unit, tr))
     ms_s, n_s, _ = prof["spread"]
     ms_c, n_c, _ = prof["crop"]
-    # 11 adjoint NFFTs of every Z-plane per outer iteration (CGNR: one before
-    # the loop, one per step); each runs the row pass once per chunk of planes
-    units = 11 * nz * steps
-    planes_per_launch = units / max(1, n_c)
-    secs = (ms_s + ms_c) / 1e3
-    achieved = units * unit / secs / 1e9
-    return "adjoint NFFT", {
-        "bound": "hbm",
-        "kernel": "adjoint NFFT (k_spread_gather + k_spread_fixup + k_colifft_fs + "
-                  "k_rowifft_crop_fs)",
+    units = (1 if toep[1] > 0 else 11) * nz * steps
+    groups.append(("adjoint NFFT",
+                   "adjoint NFFT (k_spread_gather + k_spread_fixup + k_colifft_fs + "
+                   "k_rowifft_crop_fs)", ms_s + ms_c, units, max(1, n_c),
+                   csize * (P * P + 4 * n * n + M), MEASURED_ADJOINT_TRAFFIC_PER_PLANE))
+    top, kernel, ms, units, launches, unit, tr = max(groups, key=lambda g: g[2])
+    planes_per_launch = units / launches
+    achieved = units * unit / (ms / 1e3) / 1e9
+    return top, {
+        "bound": "hbm", "kernel": kernel,
         "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
         "frac": round(achieved / peak_gbs, 4),
-        "traffic": round(MEASURED_ADJOINT_TRAFFIC_PER_PLANE * planes_per_launch),
+        "traffic": round(tr * planes_per_launch) if tr else None,
         "algorithmic_bytes_per_launch": unit * planes_per_launch,
         "algorithmic_bytes_per_unit": unit, "units_per_launch": planes_per_launch,
-        "avg_launch_ms": (ms_s + ms_c) / max(1, n_c), "peak_source": peak_kind}, shares
+        "avg_launch_ms": ms / launches, "peak_source": peak_kind,
+        "groups_ms": {g[0]: round(g[2], 3) for g in groups}}, shares
 
 
 def cpu_sample_inputs(r, nz):
@@ -893,9 +916,15 @@ def tv_micro(args):
         e1.record(st)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
+        # fused passes (FP32 default): a gradient (2 values per voxel), 39
+        # passes of 4 and an update of 3; unfused (FP64 default): 5 per inner
+        # iteration
+        env = os.environ.get("NUDIM_TV", "")
+        fused = env == "fused" or (env != "unfused" and prec == ng.MIXED)
+        per = (2 + 4 * 39 + 3) / 40.0 if fused else 5.0
         out[name] = {"ms_per_call": ms, "ms_per_inner_iteration": ms / 40,
                      "value": 40 * V / (ms / 1e3),
-                     "bytes_per_inner_iteration": 5 * (4 if prec == ng.MIXED else 8) * V}
+                     "bytes_per_inner_iteration": per * (4 if prec == ng.MIXED else 8) * V}
         log("tv %s %s: %.2f ms per 40 inner iterations" % (name, args.tv, ms))
     ctx.close()
     print(json.dumps(out))

@@ -92,7 +92,7 @@ template <typename T> struct JobState {
     NfftDev<T> pl;
     T *img_a = nullptr, *img_b = nullptr, *grad = nullptr, *w = nullptr;
     C *data = nullptr, *y = nullptr, *r = nullptr, *v = nullptr, *z = nullptr, *p = nullptr,
-      *slices = nullptr;
+      *q = nullptr, *slices = nullptr;
     int *known = nullptr;
     double *part = nullptr, *dots = nullptr, *tv_part = nullptr, *tv_scal = nullptr,
            *rh = nullptr;
@@ -149,6 +149,7 @@ struct nudim_job {
     int A = 0, M = 0, nmeas = 0, n_unk_row = 0;
     double pad_min = 0, pad_max = 0;
     NfftTables tabs;
+    std::vector<double> x;  // the M polar nodes (x[2j], x[2j+1])
     std::vector<int> known, order, unk_rank;
     std::vector<double> fill;
     bool fill_set = false, ready = false;
@@ -217,6 +218,19 @@ template <typename T> static int zfft(nudim_job *jb, JobState<T> &s, int dir)
 }
 
 // ================================================================ job state setup
+// The CGNR form of a job state: NFFT (a trafo and an adjoint per step, the
+// reference's own route and the FP64 default) or Toeplitz (one convolution
+// pass per step, the FP32 default where the plan's grid allows it);
+// NUDIM_CG=nfft|toeplitz selects one.  Read when the state is set up.
+template <typename T> static bool use_toeplitz(const NfftDev<T> &pl)
+{
+    if (!pl.toeplitz_fits()) return false;
+    const char *e = getenv("NUDIM_CG");
+    if (e && !strcmp(e, "nfft")) return false;
+    if (e && !strcmp(e, "toeplitz")) return true;
+    return sizeof(T) == 4;
+}
+
 template <typename T> static int state_init(nudim_job *jb, JobState<T> &s)
 {
     if (s.live) return NUDIM_OK;
@@ -246,6 +260,12 @@ template <typename T> static int state_init(nudim_job *jb, JobState<T> &s)
         NUDIM_CUDA(cudaMemcpyAsync(s.w, wt.data(), sizeof(T) * M, cudaMemcpyHostToDevice,
                                    jb->stream));
     }
+    if (use_toeplitz<T>(s.pl)) {
+        // CGNR's normal operator by Toeplitz embedding: T p into q
+        NUDIM_TRY(s.alloc(&s.q, V));
+        NUDIM_TRY(s.pl.toeplitz_init(jb->x.data(), s.w, jb->stream));
+        s.bytes += (size_t)s.pl.n0 * s.pl.n1 * sizeof(cplx_t<T>);
+    }
     if (jb->d.denoise == NUDIM_DENOISE_TV) {
         NUDIM_TRY(s.alloc(&s.grad, V));
         s.tv_cap = tv_part_count(nz, np, np);
@@ -268,6 +288,7 @@ template <typename T> static CgnrBuffers<T> cg_bufs(JobState<T> &s)
     b.v = s.v;
     b.z = s.z;
     b.p = s.p;
+    b.q = s.q;
     b.part = s.part;
     b.part_stride = s.part_stride;
     b.dots = s.dots;
@@ -358,8 +379,11 @@ template <typename T> static int iterate_body(nudim_job *jb, JobState<T> &s, boo
         bool h = d.height && d.variant == NUDIM_VARIANT_SERIAL;
         int ylo = (2 * d.ncenter - d.nheight) / 2, yhi = (2 * d.ncenter + d.nheight) / 2;
         ProfScope ps(jb->ctx, PK_TV, st, 40 * 5.0 * sT * (double)V);
+        // the CGNR vector z (V complex values, rewritten by every CGNR run) is
+        // free here: the fused TV passes' second volume and gradient
+        T *tv2 = reinterpret_cast<T *>(s.z);
         NUDIM_TRY(tv_run<T>(s.img_b, s.grad, s.tv_part, s.tv_cap, s.tv_scal, nz, np, np, 0.2f, 40,
-                            h ? 1 : 0, ylo, yhi, st));
+                            h ? 1 : 0, ylo, yhi, st, tv2, tv2 + V));
     }
     if (dump) {
         NUDIM_TRY(launch_to_double<T>(s.img_b, (double *)s.z, V, st));
@@ -651,6 +675,9 @@ static size_t job_bytes(const nudim_job_desc *d, int A, bool both, size_t fused_
         // spectra + grid (adjoint) of one chunk of planes
         size_t plane = (np * n1 + std::max(5 * M, n1 * n1)) * sC, chunk = fused_budget / plane;
         b += (chunk < 1 ? 1 : chunk < nz ? chunk : nz) * plane;
+        // FP32 CGNR by Toeplitz embedding (grids of 256 to 1024 points): T p
+        // and the kernel's DFT
+        if (sT == 4 && n1 >= 256 && n1 <= 1024) b += V * sC + n1 * n1 * sC;
         return b;
     };
     size_t b = d->precision == NUDIM_FP64 ? per(8) : per(4);
@@ -742,8 +769,9 @@ int nudim_profile_kernel_count(void) { return PK_COUNT; }
 
 const char *nudim_profile_kernel_name(int k)
 {
-    static const char *names[PK_COUNT] = {"pad",   "fft2d",  "interp", "spread", "crop",
-                                          "cgvec", "zfft",   "volume", "tv",     "diffusion"};
+    static const char *names[PK_COUNT] = {"pad",   "fft2d",  "interp", "spread",    "crop",
+                                          "cgvec", "zfft",   "volume", "tv",        "diffusion",
+                                          "toeplitz"};
     return (k >= 0 && k < PK_COUNT) ? names[k] : nullptr;
 }
 
@@ -810,7 +838,8 @@ int nudim_job_create(nudim_ctx *ctx, const nudim_job_desc *desc, nudim_job **out
     jb->nmeas = (int)((d.gam_max - d.gam_min) / d.interval + 0.5) + 1;
     jb->A = polar_lines(d.gam_min, d.interval, d.padangle, &jb->pad_min, &jb->pad_max);
     jb->M = jb->A * d.np;
-    std::vector<double> x((size_t)jb->M * 2);
+    std::vector<double> &x = jb->x;
+    x.resize((size_t)jb->M * 2);
     equal_angle_sample_2d(jb->pad_min, jb->pad_max, d.padangle, d.np, x.data());
     if (build_nfft_tables(d.np, d.np, jb->M, x.data(), 16, 16, &jb->tabs) != 0) {
         set_error("invalid NFFT geometry");
@@ -1446,16 +1475,22 @@ int nudim_tv(nudim_ctx *ctx, int precision, void *vol, int nz, int ny, int nx, f
     int cap = tv_part_count(nz, ny, nx);
     size_t sT = precision == NUDIM_FP64 ? 8 : 4;
     double *scr;
-    NUDIM_TRY(ctx_scratch(ctx, sizeof(double) * (cap + 4) + sT * V, &scr));
+    // partials and sums, then the gradient and the fused passes' second
+    // volume and gradient (each 256-byte aligned)
+    const size_t head = ((sizeof(double) * ((size_t)cap + 4)) + 255) & ~(size_t)255;
+    const size_t vb = (sT * V + 255) & ~(size_t)255;
+    NUDIM_TRY(ctx_scratch(ctx, head + 3 * vb, &scr));
     double *part = scr, *scal = scr + cap;
-    void *grad = (void *)(scr + cap + 4);
+    unsigned char *grad = (unsigned char *)scr + head;
     int ylo = (2 * ncenter - nheight) / 2, yhi = (2 * ncenter + nheight) / 2;
     cudaStream_t st = (cudaStream_t)stream;
     if (precision == NUDIM_FP64)
         return tv_run<double>((double *)vol, (double *)grad, part, cap, scal, nz, ny, nx, lam,
-                              niter, height ? 1 : 0, ylo, yhi, st);
+                              niter, height ? 1 : 0, ylo, yhi, st, (double *)(grad + vb),
+                              (double *)(grad + 2 * vb));
     return tv_run<float>((float *)vol, (float *)grad, part, cap, scal, nz, ny, nx, lam, niter,
-                         height ? 1 : 0, ylo, yhi, st);
+                         height ? 1 : 0, ylo, yhi, st, (float *)(grad + vb),
+                         (float *)(grad + 2 * vb));
 }
 
 int nudim_diffusion2d(nudim_ctx *ctx, int precision, void *vol, int nz, int ny, int nx,

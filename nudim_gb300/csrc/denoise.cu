@@ -7,6 +7,9 @@
 // FP32 form uses fused multiply-adds, rsqrt and fast division where noted.
 #include "engine.cuh"
 
+#include <cstdlib>
+#include <cstring>
+
 namespace nudim {
 
 // ================================================================ TV
@@ -121,11 +124,20 @@ template <typename T> struct TvAcc {
 // blocks in the FP32 form.  Grid (x tiles, y tiles, Z-runs of zc planes);
 // 256 threads, thread (ty, tx) owns the columns (j0 + ty + 8 r, k0 + tx),
 // r < kTvRows.  done: a zeroed counter (the last block resets it).
-template <typename T>
+//
+// FUSED: the previous iteration's update is applied as the tile is read
+// (u' = u - (lam sqrt(scal_in[1])) (g_in / sqrt(scal_in[0])) on every tile
+// and halo cell, with k_tv_update's operations), the owned cells' u' are
+// written to u_out and the gradient of u' to g: one pass reads u and g_in and
+// writes u' and g (4 values per voxel instead of the 5 of a gradient and an
+// update).  u_out and g must not alias u and g_in (other blocks still read
+// their halos).
+template <typename T, bool FUSED>
 __global__ void __launch_bounds__(256)
 k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part,
           unsigned *__restrict__ done, double *__restrict__ scal, int nz, int ny, int nx,
-          int zc, int height, int ylo, int yhi)
+          int zc, int height, int ylo, int yhi, const T *__restrict__ g_in,
+          const double *__restrict__ scal_in, double lam, T *__restrict__ u_out)
 {
     constexpr int kCells = kTvSY * kTvSX, kSlots = (kCells + 255) / 256;
     __shared__ T pl[3][kTvSY][kTvSX];
@@ -135,16 +147,19 @@ k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part,
     const int k0 = blockIdx.x * kTvTX, j0 = blockIdx.y * kTvTY;
     const int z0 = blockIdx.z * zc, z1 = min(nz, z0 + zc);
     const int k = k0 + tx;
-    bool own[kTvRows];
+    bool own[kTvRows], inb[kTvRows];
 #pragma unroll
     for (int r = 0; r < kTvRows; r++) {
         const int j = j0 + ty + 8 * r;
-        own[r] = k < nx && j < ny && (!height || (j >= ylo && j <= yhi));
+        inb[r] = k < nx && j < ny;
+        own[r] = inb[r] && (!height || (j >= ylo && j <= yhi));
     }
     const size_t P = (size_t)ny * nx;
-    // this thread's halo-tile cells and their clamped in-plane offsets
+    // this thread's halo-tile cells, their clamped in-plane offsets and (FUSED)
+    // whether the update applies to their row
     int cell[kSlots];
     size_t off[kSlots];
+    bool upd[kSlots];
 #pragma unroll
     for (int s = 0; s < kSlots; s++) {
         int c = threadIdx.x + 256 * s;
@@ -152,17 +167,30 @@ k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part,
         int yy = c / kTvSX, xx = c - yy * kTvSX;
         int gj = min(max(j0 + yy - 1, 0), ny - 1), gk = min(max(k0 + xx - 1, 0), nx - 1);
         off[s] = (size_t)gj * nx + gk;
+        upd[s] = !height || (gj >= ylo && gj <= yhi);
     }
-    T pre[kSlots];
+    T tn = T(1), la = T(0);
+    if (FUSED) {  // the same FP64 expressions as k_tv_update
+        tn = (T)sqrt(scal_in[0]);
+        la = (T)(lam * sqrt(scal_in[1]));
+    }
+    T pre[kSlots], preg[kSlots];
     auto fetch = [&](int plane) {
 #pragma unroll
         for (int s = 0; s < kSlots; s++)
-            if (cell[s] >= 0) pre[s] = u[(size_t)plane * P + off[s]];
+            if (cell[s] >= 0) {
+                pre[s] = u[(size_t)plane * P + off[s]];
+                if (FUSED) preg[s] = g_in[(size_t)plane * P + off[s]];
+            }
     };
     auto store = [&](int b) {
 #pragma unroll
         for (int s = 0; s < kSlots; s++)
-            if (cell[s] >= 0) (&pl[b][0][0])[cell[s]] = pre[s];
+            if (cell[s] >= 0) {
+                T v = pre[s];
+                if (FUSED && upd[s]) v = rn_sub(v, rn_mul(la, rn_div(preg[s], tn)));
+                (&pl[b][0][0])[cell[s]] = v;
+            }
     };
     int bp = 0, bc = 1, bn = 2;
     fetch(max(z0 - 1, 0));
@@ -180,15 +208,20 @@ k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part,
             const float2 g2 = tv_point2(pl[bp], pl[bc], pl[bn], ty + 1, tx + 1, c2);
             const float gv[2] = {g2.x, g2.y}, cv[2] = {c2.x, c2.y};
 #pragma unroll
-            for (int r = 0; r < 2; r++)
+            for (int r = 0; r < 2; r++) {
+                if (FUSED && inb[r]) u_out[(size_t)i * P + (size_t)(j0 + ty + 8 * r) * nx + k] = cv[r];
                 if (own[r]) {
                     g[(size_t)i * P + (size_t)(j0 + ty + 8 * r) * nx + k] = gv[r];
                     ag.add(rn_mul(gv[r], gv[r]));
                     if (cv[r] < 0.f) an.add(rn_mul(cv[r], cv[r]));
                 }
+            }
         } else {
 #pragma unroll
-            for (int r = 0; r < kTvRows; r++)
+            for (int r = 0; r < kTvRows; r++) {
+                if (FUSED && inb[r])
+                    u_out[(size_t)i * P + (size_t)(j0 + ty + 8 * r) * nx + k] =
+                        pl[bc][ty + 8 * r + 1][tx + 1];
                 if (own[r]) {
                     T c;
                     T gv = tv_point<T>(pl[bp], pl[bc], pl[bn], ty + 8 * r + 1, tx + 1, c);
@@ -196,6 +229,7 @@ k_tv_grad(const T *__restrict__ u, T *__restrict__ g, double *__restrict__ part,
                     ag.add(rn_mul(gv, gv));
                     if (c < T(0)) an.add(rn_mul(c, c));
                 }
+            }
         }
         __syncthreads();
         if (i + 1 < z1) {
@@ -240,12 +274,13 @@ template <typename T, int N> struct alignas(sizeof(T) * N) TvVec {
     T v[N];
 };
 
-// u -= (lam * sqrt(dA)) * (g / sqrt(sum g^2))   (denoise.c:125-142), VEC
-// voxels per access.  The two scalars are formed once per block (the same
-// FP64 expressions in every block, so every voxel sees the same values).
+// u_out = u - (lam * sqrt(dA)) * (g / sqrt(sum g^2))   (denoise.c:125-142),
+// VEC voxels per access; u_out may be u.  The two scalars are formed once per
+// block (the same FP64 expressions in every block, so every voxel sees the
+// same values).
 template <typename T, typename I, int VEC>
 __global__ void __launch_bounds__(256)
-k_tv_update(T *__restrict__ u, const T *__restrict__ g, const double *__restrict__ scal,
+k_tv_update(const T *u, T *u_out, const T *__restrict__ g, const double *__restrict__ scal,
             double lam, int nz, int ny, int nx, int height, int ylo, int yhi)
 {
     __shared__ T s_tn, s_la;
@@ -267,7 +302,7 @@ k_tv_update(T *__restrict__ u, const T *__restrict__ g, const double *__restrict
             }
             x.v[e] = rn_sub(x.v[e], rn_mul(la, rn_div(y.v[e], tn)));
         }
-        reinterpret_cast<TvVec<T, VEC> *>(u)[t] = x;
+        reinterpret_cast<TvVec<T, VEC> *>(u_out)[t] = x;
     }
 }
 
@@ -282,7 +317,7 @@ template <typename T> static int tv_grad_blocks_per_sm()
 {
     static const int occ = [] {
         int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tv_grad<T>, 256, 0) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tv_grad<T, true>, 256, 0) !=
                 cudaSuccess ||
             b < 1)
             b = 1;
@@ -291,10 +326,22 @@ template <typename T> static int tv_grad_blocks_per_sm()
     return occ;
 }
 
+// Fused passes (FP32 default) or a gradient and a separate update per
+// iteration (FP64 default: the FP64 gradient is bound by the FP64 pipe, and
+// the folded update made it slower than the two launches); NUDIM_TV=
+// fused|unfused selects one.  The same values bit for bit; read at every call.
+template <typename T> static bool tv_unfused()
+{
+    const char *e = getenv("NUDIM_TV");
+    if (e && !strcmp(e, "unfused")) return true;
+    if (e && !strcmp(e, "fused")) return false;
+    return sizeof(T) == 8;
+}
+
 template <typename T, typename I>
 static int tv_launch(T *u, T *grad, double *part, int part_cap, double *scal, size_t V, int nz,
                      int ny, int nx, float lam, int niter, int height, int ylo, int yhi,
-                     cudaStream_t st)
+                     T *u2, T *g2, cudaStream_t st)
 {
     int dev = 0, sms = 0;
     NUDIM_CUDA(cudaGetDevice(&dev));
@@ -313,38 +360,71 @@ static int tv_launch(T *u, T *grad, double *part, int part_cap, double *scal, si
     }
     unsigned *done = reinterpret_cast<unsigned *>(part + 2 * nb);
     NUDIM_CUDA(cudaMemsetAsync(done, 0, sizeof(unsigned), st));
-    // widest access that divides the volume and both pointers' alignment
     constexpr int W = 16 / sizeof(T);
-    const bool wide = V % W == 0 && (reinterpret_cast<uintptr_t>(u) % 16) == 0 &&
-                      (reinterpret_cast<uintptr_t>(grad) % 16) == 0;
-    const long nu = std::min((long)ceil_div((long)(wide ? V / W : V), 256), (long)sms * 8);
-    for (int it = 0; it < niter; it++) {
-        k_tv_grad<T><<<gg, 256, 0, st>>>(u, grad, part, done, scal, nz, ny, nx, zc, height, ylo,
-                                         yhi);
-        NUDIM_LAUNCH_CHECK();
-        if (wide)
-            k_tv_update<T, I, W><<<(int)nu, 256, 0, st>>>(u, grad, scal, (double)lam, nz, ny, nx,
-                                                           height, ylo, yhi);
+    const long nu1 = std::min((long)ceil_div((long)V, 256), (long)sms * 8);
+    const long nuw = std::min((long)ceil_div((long)(V / W), 256), (long)sms * 8);
+    auto wide = [&](const T *a, const T *b, const T *c) {
+        return V % W == 0 && (reinterpret_cast<uintptr_t>(a) % 16) == 0 &&
+               (reinterpret_cast<uintptr_t>(b) % 16) == 0 &&
+               (reinterpret_cast<uintptr_t>(c) % 16) == 0;
+    };
+    // u_out = u - step(g, scal): the widest access that divides the volume and
+    // the pointers' alignment
+    auto update = [&](const T *uin, T *uout, const T *gv, const double *sc) -> int {
+        if (wide(uin, uout, gv))
+            k_tv_update<T, I, W><<<(int)nuw, 256, 0, st>>>(uin, uout, gv, sc, (double)lam, nz, ny,
+                                                            nx, height, ylo, yhi);
         else
-            k_tv_update<T, I, 1><<<(int)nu, 256, 0, st>>>(u, grad, scal, (double)lam, nz, ny, nx,
-                                                           height, ylo, yhi);
+            k_tv_update<T, I, 1><<<(int)nu1, 256, 0, st>>>(uin, uout, gv, sc, (double)lam, nz, ny,
+                                                            nx, height, ylo, yhi);
         NUDIM_LAUNCH_CHECK();
+        return NUDIM_OK;
+    };
+    if (niter <= 0) return NUDIM_OK;
+    if (!u2 || !g2 || niter < 2 || tv_unfused<T>()) {
+        for (int it = 0; it < niter; it++) {
+            k_tv_grad<T, false><<<gg, 256, 0, st>>>(u, grad, part, done, scal, nz, ny, nx, zc,
+                                                    height, ylo, yhi, nullptr, nullptr, 0.0,
+                                                    nullptr);
+            NUDIM_LAUNCH_CHECK();
+            NUDIM_TRY(update(u, u, grad, scal));
+        }
+        return NUDIM_OK;
     }
-    return NUDIM_OK;
+    // fused: the gradient of u, then niter - 1 passes that update with the
+    // previous gradient and take the next one (volumes and gradients alternate
+    // between (u, grad) and (u2, g2), the sums between scal[0..1] and
+    // scal[2..3]), then the last update into u
+    k_tv_grad<T, false><<<gg, 256, 0, st>>>(u, grad, part, done, scal, nz, ny, nx, zc, height, ylo,
+                                            yhi, nullptr, nullptr, 0.0, nullptr);
+    NUDIM_LAUNCH_CHECK();
+    T *cu = u, *cg = grad;
+    double *cs = scal;
+    for (int it = 1; it < niter; it++) {
+        T *nu = cu == u ? u2 : u, *ng = cg == grad ? g2 : grad;
+        double *ns = cs == scal ? scal + 2 : scal;
+        k_tv_grad<T, true><<<gg, 256, 0, st>>>(cu, ng, part, done, ns, nz, ny, nx, zc, height, ylo,
+                                               yhi, cg, cs, (double)lam, nu);
+        NUDIM_LAUNCH_CHECK();
+        cu = nu;
+        cg = ng;
+        cs = ns;
+    }
+    return update(cu, u, cg, cs);
 }
 
 template <typename T>
 int tv_run(T *u, T *grad, double *part, int part_cap, double *scal, int nz, int ny, int nx,
-           float lam, int niter, int height, int ylo, int yhi, cudaStream_t st)
+           float lam, int niter, int height, int ylo, int yhi, cudaStream_t st, T *u2, T *g2)
 {
     size_t V = (size_t)nz * ny * nx;
     if (V == 0 || niter <= 0) return NUDIM_OK;
     // 32-bit voxel indices while index + grid stride stays below 2^32
     if (V < ((size_t)1 << 31))
         return tv_launch<T, unsigned>(u, grad, part, part_cap, scal, V, nz, ny, nx, lam, niter,
-                                      height, ylo, yhi, st);
+                                      height, ylo, yhi, u2, g2, st);
     return tv_launch<T, size_t>(u, grad, part, part_cap, scal, V, nz, ny, nx, lam, niter, height,
-                                ylo, yhi, st);
+                                ylo, yhi, u2, g2, st);
 }
 
 // ================================================================ diffusion
@@ -356,9 +436,15 @@ __device__ __forceinline__ double diff_coef(double g, double Ksq)
 {
     return rn_div(1.0, rn_add(1.0, rn_div(rn_mul(g, g), Ksq)));
 }
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ float diff_coef(float g, float Ksq)
 {
-    return __fdividef(Ksq, Ksq + g * g);
+    return Ksq * rcp_approx(fmaf(g, g, Ksq));
 }
 
 template <typename T>
@@ -594,6 +680,177 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
     }
 }
 
+// The same ring of diagonals with the work dealt out by rows instead of task
+// tables.  A slot holds a diagonal at its rows' positions (cell (y, d - y) of
+// diagonal d at position y of slot d mod R, slots ny values long), so a cell's
+// N and W sit at y - 1 and y of slot d - 1 and its S and E at y + 1 and y of
+// slot d + 1.  At step t sweep g updates row y's cell on diagonal t - 2g.  A
+// warp owns 32 consecutive rows and one of TPR sweep classes (g = class mod
+// TPR): at a given sweep its lanes touch consecutive positions of one slot
+// (no bank conflicts), and no per-step table or search is needed.  A thread
+// updates two of its cells at a time (sweeps g and g + TPR: independent,
+// their slots differ by an even number, their neighbours' by an odd one),
+// the FP32 arithmetic of the two as paired instructions.  Prefetch of
+// diagonal t + 2, write-back of the group's final diagonal and one barrier
+// per step as in k_diffusion_ring.  Requires min(ny, nx) <= kDiffPf *
+// blockDim.x, blockDim.x a multiple of 32 TPR and, FP32, blockDim.x <= 768
+// (two CTAs per SM).
+template <typename T> struct DiffNb {
+    T c, n, w, s, e;
+};
+
+// two cells at once; FP32: paired instructions with diff_cell's operations
+template <typename T>
+__device__ __forceinline__ void diff_cell2(const DiffNb<T> &a, const DiffNb<T> &b, T lambda,
+                                           T Ksq, T &ua, T &ub)
+{
+    if constexpr (sizeof(T) == 4) {
+        auto f2 = [](float x, float y) { return make_float2(x, y); };
+        auto sub = [](float2 x, float2 y) { return __fadd2_rn(x, make_float2(-y.x, -y.y)); };
+        const float2 c = f2(a.c, b.c), k2 = f2(Ksq, Ksq);
+        const float2 gN = sub(f2(a.n, b.n), c), gS = sub(f2(a.s, b.s), c),
+                     gE = sub(f2(a.e, b.e), c), gW = sub(f2(a.w, b.w), c);
+        auto coef = [&](float2 g) {
+            const float2 d = __ffma2_rn(g, g, k2);
+            return __fmul2_rn(k2, make_float2(rcp_approx(d.x), rcp_approx(d.y)));
+        };
+        float2 sum = __fmul2_rn(coef(gN), gN);
+        sum = __ffma2_rn(coef(gS), gS, sum);
+        sum = __ffma2_rn(coef(gE), gE, sum);
+        sum = __ffma2_rn(coef(gW), gW, sum);
+        const float2 u = __ffma2_rn(make_float2(lambda, lambda), sum, c);
+        ua = u.x;
+        ub = u.y;
+    } else {
+        ua = diff_cell<T>(a.c, a.n, a.s, a.e, a.w, lambda, Ksq);
+        ub = diff_cell<T>(b.c, b.n, b.s, b.e, b.w, lambda, Ksq);
+    }
+}
+
+template <typename T, int TPR>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 768 : 1024, sizeof(T) == 4 ? 2 : 1)
+k_diffusion_rows(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, int niter,
+                 int G, int R)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *ring = (T *)smraw;
+    T *U = u + (size_t)blockIdx.x * ny * nx;
+    const T lambda = (T)lambda_d, Ksq = (T)ksq_d;
+    const int D = ny + nx - 1, L = min(ny, nx);
+    auto y0 = [&](int d) { return max(0, d - (nx - 1)); };
+    auto len = [&](int d) { return min(d, ny - 1) - y0(d) + 1; };
+    // position i (row y0(d) + i) of diagonal d in the ring, and in the plane
+    auto slot = [&](int d) { return ring + (size_t)(d % R) * ny + y0(d); };
+    auto cell = [&](int d, int i) -> size_t {
+        int a = y0(d);
+        return (size_t)(a + i) * nx + (d - a - i);
+    };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cls = warp % TPR;
+    const int yfirst = (warp / TPR) * 32 + lane, ystride = blockDim.x / TPR;
+    const int dstep = (2 * TPR) % R;  // ring slots between sweeps g and g + TPR
+    // one cell's values: (y, x) of the diagonal in slot sd.  The reference's
+    // clamps (denoise.c:343-351): a clamped neighbour is the cell itself,
+    // x + 1 == nx reads 0.0; the reads a clamp replaces stay inside their
+    // slots and are discarded.
+    auto load = [&](int sd, int y, int x, bool hasN, bool hasS, int yN, int yS) {
+        const int sm = sd == 0 ? R - 1 : sd - 1, sp = sd == R - 1 ? 0 : sd + 1;
+        const T *rc = ring + sd * ny, *rm = ring + sm * ny, *rp = ring + sp * ny;
+        DiffNb<T> v;
+        v.c = rc[y];
+        const T vN = rm[yN], vW = rm[y], vS = rp[yS], vE = rp[y];
+        v.n = hasN ? vN : v.c;
+        v.w = x > 0 ? vW : v.c;
+        v.s = hasS ? vS : v.c;
+        v.e = x == nxb - 1 ? v.c : (x + 1 < nx ? vE : T(0));
+        return v;
+    };
+    for (int s0 = 0; s0 < niter; s0 += G) {
+        const int gc = min(G, niter - s0);
+        const int nsteps = D + 2 * (gc - 1);
+        for (int d = 0; d < 2 && d < D; d++) {
+            T *sd = slot(d);
+            for (int i = threadIdx.x; i < len(d); i += blockDim.x) sd[i] = U[cell(d, i)];
+        }
+        __syncthreads();
+        for (int t = 0; t < nsteps; t++) {
+            // fetch diagonal t + 2 (stored after this step's cells)
+            const int dn = t + 2;
+            const int nn = dn < D ? len(dn) : 0;
+            const int npf = (L + blockDim.x - 1) / blockDim.x;
+            T pf[kDiffPf];
+#pragma unroll
+            for (int k = 0; k < kDiffPf; k++) {
+                if (k >= npf) break;
+                const int i = threadIdx.x + k * blockDim.x;
+                pf[k] = i < nn ? U[cell(dn, i)] : T(0);
+            }
+            if (cls < gc)
+                for (int y = yfirst; y <= t && y < ny; y += ystride) {
+                    // this class's sweeps with a cell in row y: x = t - y - 2g
+                    // in [0, nx - 1] and g < gc
+                    const int ghi = min(gc - 1, (t - y) >> 1);
+                    int glo = t - y - nx + 2;
+                    glo = glo > 0 ? glo >> 1 : 0;
+                    int g = glo + ((cls - glo) % TPR + TPR) % TPR;
+                    const bool hasN = y > 0, hasS = y < ny - 1;
+                    const int yN = hasN ? y - 1 : y, yS = hasS ? y + 1 : y;
+                    int d = t - 2 * g, sd = d % R;
+                    for (; g + TPR <= ghi; g += 2 * TPR) {
+                        int sd2 = sd - dstep;
+                        if (sd2 < 0) sd2 += R;
+                        const DiffNb<T> a = load(sd, y, d - y, hasN, hasS, yN, yS);
+                        const DiffNb<T> b = load(sd2, y, d - 2 * TPR - y, hasN, hasS, yN, yS);
+                        T ua, ub;
+                        diff_cell2<T>(a, b, lambda, Ksq, ua, ub);
+                        ring[sd * ny + y] = ua;
+                        ring[sd2 * ny + y] = ub;
+                        d -= 4 * TPR;
+                        sd = sd2 - dstep;
+                        if (sd < 0) sd += R;
+                    }
+                    if (g <= ghi) {
+                        const DiffNb<T> a = load(sd, y, d - y, hasN, hasS, yN, yS);
+                        ring[sd * ny + y] = diff_cell<T>(a.c, a.n, a.s, a.e, a.w, lambda, Ksq);
+                    }
+                }
+            if (nn > 0) {
+                T *sd = slot(dn);
+#pragma unroll
+                for (int k = 0; k < kDiffPf; k++) {
+                    if (k >= npf) break;
+                    const int i = threadIdx.x + k * blockDim.x;
+                    if (i < nn) sd[i] = pf[k];
+                }
+            }
+            const int df = t - 2 * gc + 1;  // final for this group
+            if (df >= 0 && df < D) {
+                const T *sd = slot(df);
+                for (int i = threadIdx.x; i < len(df); i += blockDim.x) U[cell(df, i)] = sd[i];
+            }
+            __syncthreads();
+        }
+        {
+            const T *sd = slot(D - 1);
+            for (int i = threadIdx.x; i < len(D - 1); i += blockDim.x) U[cell(D - 1, i)] = sd[i];
+        }
+        __syncthreads();
+    }
+}
+
+// The wavefront form: rows (k_diffusion_rows, the FP32 default) or task
+// tables (k_diffusion_ring, the FP64 default: the FP64 pipe bounds both and
+// the tables form measured faster there); NUDIM_DIFFUSION=rows|tables
+// selects one.  Both give the same cells bit for bit.  Read at every launch
+// (a captured graph keeps the form it was captured with).
+template <typename T> static bool diffusion_tables()
+{
+    const char *e = getenv("NUDIM_DIFFUSION");
+    if (e && !strcmp(e, "tables")) return true;
+    if (e && !strcmp(e, "rows")) return false;
+    return sizeof(T) == 8;
+}
+
 template <typename T>
 int diffusion_run(T *u, int nz, int ny, int nx, int nx_bound, float lambda, float kappa,
                   int niter, cudaStream_t st)
@@ -602,11 +859,41 @@ int diffusion_run(T *u, int nz, int ny, int nx, int nx_bound, float lambda, floa
     double ksq = (double)kappa * (double)kappa;
     int L = ny < nx ? ny : nx;
     int P = std::min(1024, (L + 31) & ~31);
-    // FP32 on planes up to 512 wide: two diagonals at a time, two CTAs per
-    // SM; otherwise one CTA of 1024 threads with up to 160 KB of ring
+    // FP32 on planes up to 512 wide: two CTAs per SM; otherwise one CTA with
+    // up to 160 KB of ring
     bool two = sizeof(T) == 4 && P <= 512;
-    int threads = two ? 2 * P : 1024;
     const size_t budget = two ? ((size_t)108 << 10) : ((size_t)160 << 10);
+    if (!diffusion_tables<T>()) {
+        // row form: slots of ny values; TPR sweep classes (a power of two)
+        // so that 32-row warps x classes fill 768 threads (FP32, two CTAs per
+        // SM) or 1024 (FP64)
+        int G = (int)((budget / (sizeof(T) * (size_t)ny) - 2) / 2);
+        if (G > niter) G = niter;
+        if (G > kDiffMaxG) G = kDiffMaxG;
+        const int cap = sizeof(T) == 4 ? 768 : 1024, Py = (ny + 31) & ~31;
+        int tpr = 1;
+        while (tpr < 8 && 2 * tpr * Py <= cap && 2 * tpr <= G) tpr *= 2;
+        const int threads = std::min(cap, tpr * Py);
+        if (G >= 1 && L <= kDiffPf * threads) {
+            const int R = 2 * G + 2;
+            const size_t smem = sizeof(T) * (size_t)R * ny;
+#define NUDIM_DIFF_ROWS(TP)                                                                     \
+    do {                                                                                        \
+        NUDIM_CUDA(cudaFuncSetAttribute(k_diffusion_rows<T, TP>,                                \
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 160 << 10)); \
+        k_diffusion_rows<T, TP><<<nz, threads, smem, st>>>(u, ny, nx, nx_bound, (double)lambda,  \
+                                                            ksq, niter, G, R);                  \
+    } while (0)
+            if (tpr == 8) NUDIM_DIFF_ROWS(8);
+            else if (tpr == 4) NUDIM_DIFF_ROWS(4);
+            else if (tpr == 2) NUDIM_DIFF_ROWS(2);
+            else NUDIM_DIFF_ROWS(1);
+#undef NUDIM_DIFF_ROWS
+            NUDIM_LAUNCH_CHECK();
+            return NUDIM_OK;
+        }
+    }
+    int threads = two ? 2 * P : 1024;
     int G = (int)((budget / (sizeof(T) * (size_t)L) - 2) / 2);
     if (G > niter) G = niter;
     if (G > kDiffMaxG) G = kDiffMaxG;
@@ -626,9 +913,9 @@ int diffusion_run(T *u, int nz, int ny, int nx, int nx_bound, float lambda, floa
 }
 
 template int tv_run<double>(double *, double *, double *, int, double *, int, int, int, float,
-                            int, int, int, int, cudaStream_t);
+                            int, int, int, int, cudaStream_t, double *, double *);
 template int tv_run<float>(float *, float *, double *, int, double *, int, int, int, float, int,
-                           int, int, int, cudaStream_t);
+                           int, int, int, cudaStream_t, float *, float *);
 template int diffusion_run<double>(double *, int, int, int, int, float, float, int, cudaStream_t);
 template int diffusion_run<float>(float *, int, int, int, int, float, float, int, cudaStream_t);
 

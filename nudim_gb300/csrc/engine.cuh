@@ -31,6 +31,7 @@ enum ProfKernel {
     PK_VOLUME,      // pack/unpack, HIO/ER constraint, R-factor
     PK_TV,          // TV gradient + update
     PK_DIFFUSION,   // 2D anisotropic diffusion wavefront
+    PK_TOEPLITZ,    // CGNR normal operator by Toeplitz embedding (its three passes)
     PK_COUNT
 };
 struct ProfRec {
@@ -111,7 +112,9 @@ template <> constexpr int prec_of<float>() { return NUDIM_MIXED; }
 // ------------------------------------------------------------ epilogues
 enum PadMode { PM_COMPLEX = 0, PM_REAL_INIT = 1 };
 enum InterpMode { IM_PLAIN = 0, IM_RESID = 1, IM_DOTV = 2, IM_CONSTRAINT = 3 };
-enum CropMode { CM_PLAIN = 0, CM_DOT = 1, CM_INIT = 2 };
+// CM_TRESID / CM_TPDOT: the Toeplitz normal operator's row pass (no
+// deconvolution): z = out - T f, p = z, |z|^2 / q = T p, Re(p^H q)
+enum CropMode { CM_PLAIN = 0, CM_DOT = 1, CM_INIT = 2, CM_TRESID = 3, CM_TPDOT = 4 };
 
 template <typename T> struct PadArgs {
     int mode = PM_COMPLEX;
@@ -146,7 +149,8 @@ template <typename T> struct CropArgs {
     int mode = CM_PLAIN;
     cplx_t<T> *out = nullptr;
     size_t out_stride = 0;
-    cplx_t<T> *p_out = nullptr;    // CM_INIT: search direction p = z
+    cplx_t<T> *p_out = nullptr;    // CM_INIT / CM_TRESID: search direction p = z
+    const cplx_t<T> *pin = nullptr;  // CM_TPDOT: p of p^H q
     double *part = nullptr;
     int part_stride = 0;
 };
@@ -199,6 +203,23 @@ template <typename T> struct NfftDev {
     int trafo(int nplanes, const PadArgs<T> &pa, const InterpArgs<T> &ia, cudaStream_t st);
     int adjoint(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca, cudaStream_t st);
 
+    // CGNR's normal operator A^H W A by Toeplitz embedding (nfft_fused.cu):
+    // khat = the n0 x n1 DFT of its kernel K[m] = sum_j w_j e^{2 pi i m x_j},
+    // |m| < N, divided by n0 n1 and laid out in the column pass's read order;
+    // ones: N0 (or N1, the larger) unit deconvolution factors for the row passes
+    C *khat = nullptr;
+    T *ones = nullptr;
+    bool toeplitz = false;
+    bool toeplitz_fits() const
+    {
+        return fused && row_fs && N0 == N1 && n0 == n1 && (n0 == 256 || n0 == 512 || n0 == 1024);
+    }
+    // x: the M nodes (host, x[2j], x[2j+1]); w: the CGNR weights (device,
+    // nullptr: unweighted)
+    int toeplitz_init(const double *x, const T *w, cudaStream_t st);
+    // out = T src for nplanes planes of N0 x N1 (the row pass in ca's mode;
+    // pa as for trafo: PM_COMPLEX or PM_REAL_INIT)
+    int toeplitz_apply(int nplanes, const PadArgs<T> &pa, const CropArgs<T> &ca, cudaStream_t st);
     int init_fused(const NfftTables &t, cudaStream_t st);
     int autotune(const NfftTables &t, cudaStream_t st);
     void release_fused();
@@ -214,8 +235,11 @@ template <typename T> struct NfftDev {
 // z/p: planes of N0*N1.  f_zero: the start value is zero (skips A f).
 // f_real: when non-null the start value is this real array (planes of
 // N0*N1) and f is overwritten with it first.
+// q: planes of N0*N1 for T p; with it and a plan whose Toeplitz operator is
+// ready, the CG runs in coefficient space (z' = z - alpha T p, v^H W v =
+// p^H T p: the same iterates as CGNR in exact arithmetic).
 template <typename T> struct CgnrBuffers {
-    cplx_t<T> *r = nullptr, *v = nullptr, *z = nullptr, *p = nullptr;
+    cplx_t<T> *r = nullptr, *v = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
     double *part = nullptr;   // nplanes * part_stride
     int part_stride = 0;
     double *dots = nullptr;   // nplanes * 4
@@ -250,9 +274,13 @@ template <typename T>
 int launch_to_double(const T *src, double *dst, size_t n, cudaStream_t st);
 
 // ------------------------------------------------------------ denoise
+// TV-discrete, niter iterations on u in place.  scal: 4 doubles.  With u2 and
+// g2 (two more volumes, not aliasing u or grad) each iteration after the
+// first is one fused pass (the update folded into the next gradient).
 template <typename T>
 int tv_run(T *u, T *grad, double *part, int part_cap, double *scal, int nz, int ny, int nx,
-           float lam, int niter, int height, int ylo, int yhi, cudaStream_t st);
+           float lam, int niter, int height, int ylo, int yhi, cudaStream_t st,
+           T *u2 = nullptr, T *g2 = nullptr);
 int tv_part_count(int nz, int ny, int nx);
 // projection_sim -m DFT Fourier samples: dens [nz][ny][nx] (device, FP64),
 // x2 the 2D equal-angle nodes (host, (r sin g, r cos g) per node, ns*np of

@@ -19,6 +19,7 @@
 // No atomics: every output element has exactly one writer, and every sum
 // has a fixed order, so results are deterministic.
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <type_traits>
 
@@ -1098,12 +1099,26 @@ k_rowifft_crop_fs(const cplx_t<T> *__restrict__ Hp, int N0, int N1, const T *__r
                 const int c = (k1 + R1 * k2 + N1 / 2) & (n1 - 1);
                 if (c < N1) {
                     const C g = y[fs_out<R2>(k2)];
-                    const T sc = sa * c1[c];
-                    const C z = mkc<T>(g.x * sc, g.y * sc);
                     const size_t o = (size_t)gb * ca.out_stride + (size_t)a * N1 + c;
-                    ca.out[o] = z;
-                    if (MODE == CM_INIT) ca.p_out[o] = z;
-                    s += z.x * z.x + z.y * z.y;
+                    if (MODE == CM_TRESID) {
+                        // z = b - T f (b in out), p = z
+                        const C bv = ca.out[o];
+                        const C z = mkc<T>(bv.x - g.x, bv.y - g.y);
+                        ca.out[o] = z;
+                        ca.p_out[o] = z;
+                        s += z.x * z.x + z.y * z.y;
+                    } else if (MODE == CM_TPDOT) {
+                        // q = T p, Re(p^H q)
+                        const C pv = ca.pin[o];
+                        ca.out[o] = g;
+                        s += pv.x * g.x + pv.y * g.y;
+                    } else {
+                        const T sc = sa * c1[c];
+                        const C z = mkc<T>(g.x * sc, g.y * sc);
+                        ca.out[o] = z;
+                        if (MODE == CM_INIT) ca.p_out[o] = z;
+                        s += z.x * z.x + z.y * z.y;
+                    }
                 }
             }
         }
@@ -1173,6 +1188,129 @@ k_colifft_fs(const cplx_t<T> *__restrict__ G, int N0, int n1, const cplx_t<T> *_
             if (a < N0) Hb[(size_t)a * n1] = y[fs_out<R2>(k2)];
         }
     }
+}
+
+// ================================================================ Toeplitz column pass
+// CGNR's normal operator T = A^H W A is a convolution on the N0 x N1
+// coefficients: (T p)[k] = sum_k' K[k - k'] p[k'], K[m] = sum_j w_j
+// e^{2 pi i m x_j}, |m| < N.  Embedded in the n0 x n1 circulant (n >= 2N - 1,
+// so no wrap reaches a kept output) it is a pointwise product of DFTs: row
+// FFT of the zero-padded rows (K1' with unit factors), then per column the
+// n0-point FFT, the product with khat (the kernel's DFT / (n0 n1)) and the
+// inverse FFT, keeping the N0 rows (this kernel), then the inverse row FFT
+// with the crop (K5' with unit factors).  One CTA per (4-column block,
+// plane), R2 threads per column: pass 1 as in k_colfft_interp_fs; pass 2
+// leaves thread k1 with Y[k1 + R1 k2] for all k2, which is the first
+// (R2-point, over k2) step of the inverse four-step FFT: its outputs t2 are
+// twiddled by e^{+2 pi i k1 t2 / n0} and exchanged, and thread t2 finishes
+// with the R1-point DFT over k1 (output row t2 + R2 t1).  The exchange buffer
+// is reused for the inverse (one barrier between the last read and the first
+// write).  In place: the CTA reads and writes the same N0 x 4 values of H.
+template <typename T, int R1, int R2>
+__global__ void __launch_bounds__(4 * R2)
+k_col_toeplitz(cplx_t<T> *__restrict__ H, int N0, int n1, const cplx_t<T> *__restrict__ tw0,
+               const cplx_t<T> *__restrict__ khat)
+{
+    using C = cplx_t<T>;
+    constexpr int n0 = R1 * R2, BC = 4, CS = fs_col_stride<R1, R2>(), KI = R1 / R2;
+    static_assert(R2 * (R1 + 1) <= CS, "inverse exchange exceeds the column stride");
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *S = (C *)smraw;
+    const int cb = blockIdx.x, b = blockIdx.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = lane & 3, j = warp * 8 + (lane >> 2);
+    C *Hb = H + (size_t)b * N0 * n1 + (size_t)cb * BC + c;
+    {
+        C x[R1];
+#pragma unroll
+        for (int m = 0; m < R1; m++) {
+            const int l0 = j + R2 * m;
+            const int a = (l0 < n0 / 2 ? l0 : l0 - n0) + N0 / 2;
+            x[m] = (a >= 0 && a < N0) ? Hb[(size_t)a * n1] : mkc<T>(0, 0);
+        }
+        fs_dft<T, -1, R1>(x);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) {
+            C v = x[fs_out<R1>(k1)];
+            if (k1) v = cmul<T>(v, tw0[j * k1]);
+            S[c * CS + k1 * (R2 + 1) + j] = v;
+        }
+    }
+    __syncthreads();
+    C y[KI][R2];
+#pragma unroll
+    for (int i = 0; i < KI; i++)
+#pragma unroll
+        for (int jj = 0; jj < R2; jj++) y[i][jj] = S[c * CS + (j + R2 * i) * (R2 + 1) + jj];
+    __syncthreads();  // S is reused for the inverse exchange
+#pragma unroll
+    for (int i = 0; i < KI; i++) {
+        const int k1 = j + R2 * i;
+        fs_dft<T, -1, R2>(y[i]);
+        C z[R2];
+        const C *kp = khat + (((size_t)cb * R2) * R1 + k1) * BC + c;
+#pragma unroll
+        for (int k2 = 0; k2 < R2; k2++)
+            z[k2] = cmul<T>(y[i][fs_out<R2>(k2)], kp[(size_t)k2 * R1 * BC]);
+        fs_dft<T, +1, R2>(z);
+#pragma unroll
+        for (int t2 = 0; t2 < R2; t2++) {
+            C v = z[fs_out<R2>(t2)];
+            if (k1 * t2) {
+                C w = tw0[k1 * t2];
+                w.y = -w.y;  // inverse: e^{+2 pi i k1 t2 / n0}
+                v = cmul<T>(v, w);
+            }
+            S[c * CS + t2 * (R1 + 1) + k1] = v;
+        }
+    }
+    __syncthreads();
+    {
+        const int t2 = j;
+        C w[R1];
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) w[k1] = S[c * CS + t2 * (R1 + 1) + k1];
+        fs_dft<T, +1, R1>(w);
+#pragma unroll
+        for (int t1 = 0; t1 < R1; t1++) {
+            const int a = (t2 + R2 * t1 + N0 / 2) & (n0 - 1);
+            if (a < N0) Hb[(size_t)a * n1] = w[fs_out<R1>(t1)];
+        }
+    }
+}
+
+// The kernel's four N0 x N1 quadrants K[k + s_q] (s_q = (+-N0/2, +-N1/2),
+// quadrant q = 2 (s0 > 0) + (s1 > 0), k in [-N/2, N/2)) into the n0 x n1
+// circulant c[m mod n] for |m| < N (zero elsewhere: c is zeroed first).
+template <typename T>
+__global__ void k_toep_embed(const cplx_t<T> *__restrict__ Kq, int N0, int N1, int n0, int n1,
+                             cplx_t<T> *__restrict__ circ)
+{
+    const size_t N = (size_t)N0 * N1;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 4 * N) return;
+    const int q = (int)(i / N), r = (int)(i - (size_t)q * N);
+    const int a = r / N1, cc = r - a * N1;
+    const int m0 = a - N0 / 2 + ((q >> 1) ? N0 / 2 : -N0 / 2);
+    const int m1 = cc - N1 / 2 + ((q & 1) ? N1 / 2 : -N1 / 2);
+    if (m0 <= -N0 || m0 >= N0 || m1 <= -N1 || m1 >= N1) return;
+    circ[(size_t)(m0 & (n0 - 1)) * n1 + (m1 & (n1 - 1))] = Kq[i];
+}
+
+// The circulant's DFT (row-major n0 x n1) divided by n0 n1, in the order
+// k_col_toeplitz<R1, R2> reads it: [block of 4 columns][k2][k1][column],
+// frequency row l0 = k1 + R1 k2.
+template <typename T>
+__global__ void k_toep_layout(const cplx_t<T> *__restrict__ F, int n0, int n1, int R1, int R2,
+                              cplx_t<T> *__restrict__ khat)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)n0 * n1) return;
+    const int l0 = (int)(i / n1), l1 = (int)(i - (size_t)l0 * n1);
+    const int k1 = l0 % R1, k2 = l0 / R1, cb = l1 >> 2, c = l1 & 3;
+    const T s = T(1) / ((T)n0 * (T)n1);
+    const cplx_t<T> v = F[i];
+    khat[(((size_t)cb * R2 + k2) * R1 + k1) * 4 + c] = mkc<T>(v.x * s, v.y * s);
 }
 
 // ================================================================ K4b column IFFT
@@ -1444,6 +1582,10 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_DOT, R1, R2>,                        \
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, L));           \
     NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_INIT, R1, R2>,                       \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, L));           \
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_TRESID, R1, R2>,                     \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, L));           \
+    NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_TPDOT, R1, R2>,                      \
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, L))
         NUDIM_ROWFS_ATTR(32, 32, lr1);
         NUDIM_ROWFS_ATTR(32, 16, lr2);
@@ -1469,6 +1611,15 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     NUDIM_CUDA(cudaFuncSetAttribute(k_colfft_interp_fs<T, 16, 16>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, lim_col));
     // the four-step column IFFTs' exchange buffers (FP64 1024 points: 68 KB)
+    NUDIM_CUDA(cudaFuncSetAttribute(k_col_toeplitz<T, 32, 32>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(C) * 4 * fs_col_stride<32, 32>())));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_col_toeplitz<T, 32, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(C) * 4 * fs_col_stride<32, 16>())));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_col_toeplitz<T, 16, 16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(C) * 4 * fs_col_stride<16, 16>())));
     NUDIM_CUDA(cudaFuncSetAttribute(k_colifft_fs<T, 32, 32>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)(sizeof(C) * 4 * fs_col_stride<32, 32>())));
@@ -1495,7 +1646,10 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
 template <typename T> void NfftDev<T>::release_fused()
 {
     void *ptrs[] = {tw0,    tw1,  blk_off, ent,  nslots, band_off, band_node,
-                    units,  band_w, e_rb, e_cc, e_qa, e_q1, fixups};
+                    units,  band_w, e_rb, e_cc, e_qa, e_q1, fixups, khat, ones};
+    khat = nullptr;
+    ones = nullptr;
+    toeplitz = false;
     for (void *q : ptrs)
         if (q) cudaFreeAsync(q, ast);
     tw0 = tw1 = nullptr;
@@ -1796,6 +1950,177 @@ template <typename T> int NfftDev<T>::autotune(const NfftTables &t, cudaStream_t
     return NUDIM_OK;
 }
 
+// ================================================================ Toeplitz operator
+// K[m] for m in [-N, N)^2 as four adjoint NFFTs of the modulated weights
+// w_j e^{2 pi i s.x_j} (quadrant shifts s = (+-N0/2, +-N1/2): the adjoint
+// gives sum_j w_j e^{2 pi i s.x_j} e^{2 pi i k.x_j} = K[k + s] for k in
+// [-N/2, N/2)), the circulant embedding, its n0 x n1 DFT (cuFFT, once per
+// plan) and the column pass's layout.  In the plan's precision.
+template <typename T> int NfftDev<T>::toeplitz_init(const double *x, const T *w, cudaStream_t st)
+{
+    if (!toeplitz_fits()) {
+        set_error("Toeplitz operator: needs the fused four-step path on a square grid of 256, 512 "
+                  "or 1024 points");
+        return NUDIM_EINVAL;
+    }
+    if (toeplitz) return NUDIM_OK;
+    const double two_pi = 6.283185307179586;
+    const size_t N = (size_t)N0 * N1, nn = (size_t)n0 * n1;
+    std::vector<C> hv(4 * (size_t)M);
+    for (int q = 0; q < 4; q++) {
+        const double s0 = (q >> 1) ? N0 / 2 : -N0 / 2, s1 = (q & 1) ? N1 / 2 : -N1 / 2;
+        for (int j = 0; j < M; j++) {
+            // the phase's fractional part first: |s.x| reaches N/2 turns
+            double ph = s0 * x[2 * (size_t)j] + s1 * x[2 * (size_t)j + 1];
+            ph -= std::floor(ph);
+            hv[(size_t)q * M + j] = mkc<T>((T)std::cos(two_pi * ph), (T)std::sin(two_pi * ph));
+        }
+    }
+    std::vector<T> hones(std::max(N0, N1), T(1));
+    void *dv = nullptr, *dk = nullptr, *dc = nullptr, *d1 = nullptr, *kh = nullptr;
+    // temporaries released stream-ordered after their last use; on failure
+    // the kept buffers too
+    auto done = [&](int e) {
+        for (void *q : {dv, dk, dc})
+            if (q) cudaFreeAsync(q, st);
+        if (e) {
+            if (d1) cudaFreeAsync(d1, st);
+            if (kh) cudaFreeAsync(kh, st);
+        }
+        return e;
+    };
+    int rc = upload_async(&dv, hv.data(), sizeof(C) * hv.size(), st);
+    if (!rc) rc = upload_async(&d1, hones.data(), sizeof(T) * hones.size(), st);
+    if (rc) return done(rc);
+    if (cudaMallocAsync(&dk, sizeof(C) * 4 * N, st) != cudaSuccess ||
+        cudaMallocAsync(&dc, sizeof(C) * nn, st) != cudaSuccess ||
+        cudaMallocAsync(&kh, sizeof(C) * nn, st) != cudaSuccess) {
+        set_error("Toeplitz operator: out of device memory");
+        return done(NUDIM_ECUDA);
+    }
+    SpreadArgs<T> sa;
+    sa.f = (const C *)dv;
+    sa.f_stride = M;
+    sa.w = w;
+    CropArgs<T> ca;
+    ca.mode = CM_PLAIN;
+    ca.out = (C *)dk;
+    ca.out_stride = N;
+    if ((rc = adjoint(4, sa, ca, st))) return done(rc);
+    if (cudaMemsetAsync(dc, 0, sizeof(C) * nn, st) != cudaSuccess) {
+        set_error("Toeplitz operator: memset failed");
+        return done(NUDIM_ECUDA);
+    }
+    k_toep_embed<T><<<(unsigned)ceil_div((long)(4 * N), 256), 256, 0, st>>>(
+        (const C *)dk, N0, N1, n0, n1, (C *)dc);
+    ++g_launches;
+    cufftHandle h;
+    if ((rc = ctx_fft2d(ctx, n0, n1, 1, prec_of<T>(), &h))) return done(rc);
+    if (cufftSetStream(h, st) != CUFFT_SUCCESS) {
+        set_error("Toeplitz operator: cufftSetStream failed");
+        return done(NUDIM_ECUDA);
+    }
+    if ((rc = fft_exec<T>(h, (C *)dc, CUFFT_FORWARD))) return done(rc);
+    // the column pass's four-step split of n0
+    const int R1 = n0 == 256 ? 16 : 32, R2 = n0 / R1;
+    k_toep_layout<T><<<(unsigned)ceil_div((long)nn, 256), 256, 0, st>>>((const C *)dc, n0, n1, R1,
+                                                                         R2, (C *)kh);
+    ++g_launches;
+    if (cudaGetLastError() != cudaSuccess) {
+        set_error("Toeplitz operator: setup kernel launch failed");
+        return done(NUDIM_ECUDA);
+    }
+    done(NUDIM_OK);
+    khat = (C *)kh;
+    ones = (T *)d1;
+    bytes += sizeof(C) * nn + sizeof(T) * hones.size();
+    toeplitz = true;
+    return NUDIM_OK;
+}
+
+// out = T src over nplanes planes: row FFT of the zero-padded rows (unit
+// factors), the column pass, the inverse row FFT with the crop in ca's mode.
+// Scratch: one N0 x n1 plane of row spectra per plane of a chunk.
+template <typename T>
+int NfftDev<T>::toeplitz_apply(int nplanes, const PadArgs<T> &pa, const CropArgs<T> &ca,
+                               cudaStream_t st)
+{
+    if (!toeplitz) {
+        set_error("Toeplitz operator not initialised");
+        return NUDIM_ESTATE;
+    }
+    int chunk = fused_chunk(nplanes, (size_t)N0 * n1);
+    void *wsv;
+    size_t nH = (size_t)N0 * n1 * chunk;
+    NUDIM_TRY(workspace(sizeof(C) * nH, &wsv));
+    C *H = (C *)wsv;
+    const double c = sizeof(C);
+    const size_t smem_t = sizeof(C) * 4 *
+                          (n0 == 1024 ? fs_col_stride<32, 32>() : n0 == 512 ? fs_col_stride<32, 16>()
+                                                                            : fs_col_stride<16, 16>());
+    for (int p0 = 0; p0 < nplanes; p0 += chunk) {
+        int nb = std::min(chunk, nplanes - p0);
+        {
+            ProfScope ps(ctx, PK_TOEPLITZ, st, nb * c * ((double)N0 * N1 + (double)N0 * n1));
+            dim3 g(ceil_div(N0, rows), nb);
+#define NUDIM_TROW(MD, R1, R2)                                                                   \
+    k_rowfft_fs<T, MD, R1, R2><<<g, 128, smem_row, st>>>(pa.src, pa.src_stride, N0, N1, ones,    \
+                                                          ones, tw1, p0, H, pa.f_init,          \
+                                                          pa.f_stride)
+            if (pa.mode == PM_COMPLEX) {
+                if (n1 == 1024) NUDIM_TROW(PM_COMPLEX, 32, 32);
+                else if (n1 == 512) NUDIM_TROW(PM_COMPLEX, 32, 16);
+                else NUDIM_TROW(PM_COMPLEX, 16, 16);
+            } else {
+                if (n1 == 1024) NUDIM_TROW(PM_REAL_INIT, 32, 32);
+                else if (n1 == 512) NUDIM_TROW(PM_REAL_INIT, 32, 16);
+                else NUDIM_TROW(PM_REAL_INIT, 16, 16);
+            }
+#undef NUDIM_TROW
+            NUDIM_LAUNCH_CHECK();
+        }
+        {
+            // H read and written in place; khat (n0 n1 values) read per plane
+            ProfScope ps(ctx, PK_TOEPLITZ, st, nb * c * 2.0 * N0 * n1 + c * (double)n0 * n1);
+            if (n0 == 1024)
+                k_col_toeplitz<T, 32, 32><<<dim3(n1 / 4, nb), 128, smem_t, st>>>(H, N0, n1, tw0,
+                                                                                  khat);
+            else if (n0 == 512)
+                k_col_toeplitz<T, 32, 16><<<dim3(n1 / 4, nb), 64, smem_t, st>>>(H, N0, n1, tw0,
+                                                                                 khat);
+            else
+                k_col_toeplitz<T, 16, 16><<<dim3(n1 / 4, nb), 64, smem_t, st>>>(H, N0, n1, tw0,
+                                                                                 khat);
+            NUDIM_LAUNCH_CHECK();
+        }
+        {
+            ProfScope ps(ctx, PK_TOEPLITZ, st, nb * c * ((double)N0 * n1 + 2.0 * N0 * N1));
+            dim3 g(ceil_div(N0, rows), nb);
+#define NUDIM_TCROP(MD, R1, R2)                                                                  \
+    k_rowifft_crop_fs<T, MD, R1, R2><<<g, 128, smem_row, st>>>(H, N0, N1, ones, ones, tw1, p0, ca)
+#define NUDIM_TCROP_N(MD)                                                                        \
+    do {                                                                                        \
+        if (n1 == 1024) NUDIM_TCROP(MD, 32, 32);                                                \
+        else if (n1 == 512) NUDIM_TCROP(MD, 32, 16);                                            \
+        else NUDIM_TCROP(MD, 16, 16);                                                           \
+    } while (0)
+            if (ca.mode == CM_TRESID) NUDIM_TCROP_N(CM_TRESID);
+            else if (ca.mode == CM_TPDOT) NUDIM_TCROP_N(CM_TPDOT);
+            else NUDIM_TCROP_N(CM_PLAIN);
+#undef NUDIM_TCROP_N
+#undef NUDIM_TCROP
+            NUDIM_LAUNCH_CHECK();
+        }
+    }
+    return NUDIM_OK;
+}
+
+template int NfftDev<double>::toeplitz_init(const double *, const double *, cudaStream_t);
+template int NfftDev<float>::toeplitz_init(const double *, const float *, cudaStream_t);
+template int NfftDev<double>::toeplitz_apply(int, const PadArgs<double> &,
+                                             const CropArgs<double> &, cudaStream_t);
+template int NfftDev<float>::toeplitz_apply(int, const PadArgs<float> &, const CropArgs<float> &,
+                                            cudaStream_t);
 template int NfftDev<double>::autotune(const NfftTables &, cudaStream_t);
 template int NfftDev<float>::autotune(const NfftTables &, cudaStream_t);
 template void NfftDev<double>::release_fused();

@@ -52,6 +52,127 @@ k_cg_pupdate(cplx_t<T> *__restrict__ p, const cplx_t<T> *__restrict__ z,
     p[o] = mkc<T>(beta * pv.x + zv.x, beta * pv.y + zv.y);
 }
 
+// The coefficient-space step of the Toeplitz form: alpha = |z|^2 / p^H T p;
+// f += alpha p; z -= alpha q (q = T p); per-block partial of |z'|^2.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_cgt_update(cplx_t<T> *__restrict__ f, const cplx_t<T> *__restrict__ p, cplx_t<T> *__restrict__ z,
+             const cplx_t<T> *__restrict__ q, const double *__restrict__ dots, int cur, int N,
+             double *__restrict__ part, int part_stride)
+{
+    __shared__ T s_alpha;
+    __shared__ double sh[32];
+    const int b = blockIdx.y;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (threadIdx.x == 0) s_alpha = (T)(dots[b * 4 + cur] / dots[b * 4 + 2]);
+    __syncthreads();
+    const T alpha = s_alpha;
+    T s = 0;
+    if (i < (size_t)N) {
+        const size_t o = (size_t)b * N + i;
+        cplx_t<T> fv = f[o], zv = z[o];
+        const cplx_t<T> pv = p[o], qv = q[o];
+        fv.x += alpha * pv.x;
+        fv.y += alpha * pv.y;
+        zv.x -= alpha * qv.x;
+        zv.y -= alpha * qv.y;
+        f[o] = fv;
+        z[o] = zv;
+        s = zv.x * zv.x + zv.y * zv.y;
+    }
+    const double d = block_sum_t<T>(s, sh);
+    if (threadIdx.x == 0) part[(size_t)b * part_stride + blockIdx.x] = d;
+}
+
+// CGNR with the normal operator T = A^H W A applied by Toeplitz embedding:
+// z0 = A^H W y - T f0 (one adjoint NFFT), then per step q = T p with p^H q
+// (= v^H W v for v = A p), f += alpha p, z -= alpha q (= A^H W r after
+// r -= alpha v), p = z + beta p: the iterates of cgnr_run's NFFT form in
+// exact arithmetic, one operator pass per step instead of a trafo and an
+// adjoint.
+template <typename T>
+static int cgnr_run_toeplitz(NfftDev<T> &pl, int nplanes, const cplx_t<T> *y, const T *w,
+                             cplx_t<T> *f, const T *f_real, bool f_zero, int iters,
+                             CgnrBuffers<T> &b, cudaStream_t st)
+{
+    using C = cplx_t<T>;
+    const int N = pl.N0 * pl.N1;
+    SpreadArgs<T> sa;
+    sa.f = y;
+    sa.f_stride = pl.M;
+    sa.w = w;
+    if (f_zero) {
+        NUDIM_CUDA(cudaMemsetAsync(f, 0, sizeof(C) * (size_t)N * nplanes, st));
+        CropArgs<T> ca;
+        ca.mode = CM_INIT;
+        ca.out = b.z;
+        ca.out_stride = N;
+        ca.p_out = b.p;
+        ca.part = b.part;
+        ca.part_stride = b.part_stride;
+        NUDIM_TRY(pl.adjoint(nplanes, sa, ca, st));
+    } else {
+        CropArgs<T> ca;
+        ca.mode = CM_PLAIN;
+        ca.out = b.z;
+        ca.out_stride = N;
+        NUDIM_TRY(pl.adjoint(nplanes, sa, ca, st));
+        PadArgs<T> pa;
+        if (f_real) {
+            pa.mode = PM_REAL_INIT;
+            pa.src = f_real;
+            pa.f_init = f;
+            pa.f_stride = N;
+        } else {
+            pa.src = f;
+        }
+        pa.src_stride = N;
+        CropArgs<T> cr;
+        cr.mode = CM_TRESID;
+        cr.out = b.z;
+        cr.out_stride = N;
+        cr.p_out = b.p;
+        cr.part = b.part;
+        cr.part_stride = b.part_stride;
+        NUDIM_TRY(pl.toeplitz_apply(nplanes, pa, cr, st));
+    }
+    launch_finish_sums(b.part, pl.crop_blocks(), nplanes, b.part_stride, b.dots + 0, 4, 1, st);
+    NUDIM_LAUNCH_CHECK();
+    int cur = 0;
+    for (int it = 0; it < iters; it++) {
+        PadArgs<T> pa;
+        pa.src = b.p;
+        pa.src_stride = N;
+        CropArgs<T> cq;
+        cq.mode = CM_TPDOT;
+        cq.out = b.q;
+        cq.out_stride = N;
+        cq.pin = b.p;
+        cq.part = b.part;
+        cq.part_stride = b.part_stride;
+        NUDIM_TRY(pl.toeplitz_apply(nplanes, pa, cq, st));
+        launch_finish_sums(b.part, pl.crop_blocks(), nplanes, b.part_stride, b.dots + 2, 4, 1, st);
+        const int nxt = 1 - cur;
+        {
+            ProfScope ps(pl.ctx, PK_CGVEC, st, 6.0 * sizeof(C) * (double)N * nplanes);
+            dim3 gu(ceil_div(N, 256), nplanes);
+            k_cgt_update<T><<<gu, 256, 0, st>>>(f, b.p, b.z, b.q, b.dots, cur, N, b.part,
+                                                b.part_stride);
+            NUDIM_LAUNCH_CHECK();
+            launch_finish_sums(b.part, ceil_div(N, 256), nplanes, b.part_stride, b.dots + nxt, 4,
+                               1, st);
+        }
+        {
+            ProfScope ps(pl.ctx, PK_CGVEC, st, 3.0 * sizeof(C) * (double)N * nplanes);
+            dim3 gp(ceil_div(N, 256), nplanes);
+            k_cg_pupdate<T><<<gp, 256, 0, st>>>(b.p, b.z, b.dots, cur, nxt, N);
+            NUDIM_LAUNCH_CHECK();
+        }
+        cur = nxt;
+    }
+    return NUDIM_OK;
+}
+
 int cgnr_part_stride(int M, int N)
 {
     int a = 2 * ceil_div(M, 256), b = ceil_div(N, 256);
@@ -63,6 +184,8 @@ int cgnr_run(NfftDev<T> &pl, int nplanes, const cplx_t<T> *y, const T *w, cplx_t
              const T *f_real, bool f_zero, int iters, CgnrBuffers<T> &b, cudaStream_t st)
 {
     using C = cplx_t<T>;
+    if (b.q && pl.toeplitz)
+        return cgnr_run_toeplitz<T>(pl, nplanes, y, w, f, f_real, f_zero, iters, b, st);
     int N = pl.N0 * pl.N1, M = pl.M;
     // ---- solver_before_loop: r = y - A f; z = A^H W r; p = z
     if (f_real) {

@@ -36,9 +36,11 @@ def test_footprint_and_validation(nudim_built):
     assert 3e9 < b < 8e9
     bm = nudim_built.footprint(nx=384, nz=256, np=384, gam_min=-60, gam_max=60, interval=2,
                                nhio=50, ner=50, denoise=2, precision=1)
-    # the volume-sized buffers halve; the fused pass's scratch is capped by the
-    # same budget (NUDIM_FUSED_BUDGET_MB) in both forms
-    assert bm < 0.7 * b
+    # the volume-sized buffers halve (the FP32 form holds one more complex
+    # volume, T p of its Toeplitz CGNR, and the kernel's DFT); the fused
+    # pass's scratch is capped by the same budget (NUDIM_FUSED_BUDGET_MB) in
+    # both forms
+    assert bm < 0.76 * b
     with pytest.raises(nudim_built.NudimError) as e:
         nudim_built.footprint(nx=64, nz=63, np=64, gam_min=-60, gam_max=60, interval=3)
     assert e.value.code == -1

@@ -29,8 +29,9 @@ def run_alone(nudim_built, ctx, proj, kw):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_results_equal_alone_and_in_the_mix(gpu_ctx, nudim_built, precision):
+    # the last job's 256-point grid runs the FP32 CGNR by Toeplitz embedding
     specs = [(32, 16, 40, 60, 3, 1), (24, 32, 32, 45, 1, 2), (48, 16, 56, 70, 2, 3),
-             (32, 48, 40, 60, 2, 4), (16, 16, 24, 50, 1, 5)]
+             (32, 48, 40, 60, 2, 4), (16, 16, 24, 50, 1, 5), (64, 16, 128, 60, 3, 6)]
     jobs = []
     for n, nz, npx, gmax, step, seed in specs:
         proj, kw = job_inputs(nudim_built, gpu_ctx, n, nz, npx, gmax, step, seed)
