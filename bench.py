@@ -218,8 +218,11 @@ MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((172.924160e6 + 216.713216e6)    # k_sprea
                                       + (268.486656e6 + 75.897088e6)   # k_colifft_fs
                                       + (100.737792e6 + 36.037120e6)) / 32  # k_rowifft_crop
 # The same for the Toeplitz operator pass (k_rowfft_fs + k_col_toeplitz +
-# k_rowifft_crop_fs in its p^H q mode), None until captured.
-MEASURED_TOEPLITZ_TRAFFIC_PER_PLANE = None
+# k_rowifft_crop_fs in its p^H q mode), 32-plane launches: the 100 MB of row
+# spectra between the passes stay partly in the 129 MB L2 at that size.
+MEASURED_TOEPLITZ_TRAFFIC_PER_PLANE = ((37.8e6 + 36.6e6)      # k_rowfft_fs
+                                       + (109.1e6 + 42.6e6)   # k_col_toeplitz
+                                       + (138.5e6 + 15.6e6)) / 32  # k_rowifft_crop_fs
 
 
 def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):

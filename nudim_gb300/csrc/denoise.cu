@@ -9,6 +9,7 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 namespace nudim {
 
@@ -687,10 +688,9 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
 // slot d + 1.  At step t sweep g updates row y's cell on diagonal t - 2g.  A
 // warp owns 32 consecutive rows and one of TPR sweep classes (g = class mod
 // TPR): at a given sweep its lanes touch consecutive positions of one slot
-// (no bank conflicts), and no per-step table or search is needed.  A thread
-// updates two of its cells at a time (sweeps g and g + TPR: independent,
-// their slots differ by an even number, their neighbours' by an odd one),
-// the FP32 arithmetic of the two as paired instructions.  Prefetch of
+// (no bank conflicts), and no per-step table or search is needed.  (Tried
+// and slower, measured: classes re-dealt per step to the rows a step has,
+// and two cells per iteration with paired FP32 arithmetic.)  Prefetch of
 // diagonal t + 2, write-back of the group's final diagonal and one barrier
 // per step as in k_diffusion_ring.  Requires min(ny, nx) <= kDiffPf *
 // blockDim.x, blockDim.x a multiple of 32 TPR and, FP32, blockDim.x <= 768
@@ -698,34 +698,6 @@ k_diffusion_ring(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
 template <typename T> struct DiffNb {
     T c, n, w, s, e;
 };
-
-// two cells at once; FP32: paired instructions with diff_cell's operations
-template <typename T>
-__device__ __forceinline__ void diff_cell2(const DiffNb<T> &a, const DiffNb<T> &b, T lambda,
-                                           T Ksq, T &ua, T &ub)
-{
-    if constexpr (sizeof(T) == 4) {
-        auto f2 = [](float x, float y) { return make_float2(x, y); };
-        auto sub = [](float2 x, float2 y) { return __fadd2_rn(x, make_float2(-y.x, -y.y)); };
-        const float2 c = f2(a.c, b.c), k2 = f2(Ksq, Ksq);
-        const float2 gN = sub(f2(a.n, b.n), c), gS = sub(f2(a.s, b.s), c),
-                     gE = sub(f2(a.e, b.e), c), gW = sub(f2(a.w, b.w), c);
-        auto coef = [&](float2 g) {
-            const float2 d = __ffma2_rn(g, g, k2);
-            return __fmul2_rn(k2, make_float2(rcp_approx(d.x), rcp_approx(d.y)));
-        };
-        float2 sum = __fmul2_rn(coef(gN), gN);
-        sum = __ffma2_rn(coef(gS), gS, sum);
-        sum = __ffma2_rn(coef(gE), gE, sum);
-        sum = __ffma2_rn(coef(gW), gW, sum);
-        const float2 u = __ffma2_rn(make_float2(lambda, lambda), sum, c);
-        ua = u.x;
-        ub = u.y;
-    } else {
-        ua = diff_cell<T>(a.c, a.n, a.s, a.e, a.w, lambda, Ksq);
-        ub = diff_cell<T>(b.c, b.n, b.s, b.e, b.w, lambda, Ksq);
-    }
-}
 
 template <typename T, int TPR>
 __global__ void __launch_bounds__(sizeof(T) == 4 ? 768 : 1024, sizeof(T) == 4 ? 2 : 1)
@@ -796,22 +768,12 @@ k_diffusion_rows(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
                     const bool hasN = y > 0, hasS = y < ny - 1;
                     const int yN = hasN ? y - 1 : y, yS = hasS ? y + 1 : y;
                     int d = t - 2 * g, sd = d % R;
-                    for (; g + TPR <= ghi; g += 2 * TPR) {
-                        int sd2 = sd - dstep;
-                        if (sd2 < 0) sd2 += R;
-                        const DiffNb<T> a = load(sd, y, d - y, hasN, hasS, yN, yS);
-                        const DiffNb<T> b = load(sd2, y, d - 2 * TPR - y, hasN, hasS, yN, yS);
-                        T ua, ub;
-                        diff_cell2<T>(a, b, lambda, Ksq, ua, ub);
-                        ring[sd * ny + y] = ua;
-                        ring[sd2 * ny + y] = ub;
-                        d -= 4 * TPR;
-                        sd = sd2 - dstep;
-                        if (sd < 0) sd += R;
-                    }
-                    if (g <= ghi) {
+                    for (; g <= ghi; g += TPR) {
                         const DiffNb<T> a = load(sd, y, d - y, hasN, hasS, yN, yS);
                         ring[sd * ny + y] = diff_cell<T>(a.c, a.n, a.s, a.e, a.w, lambda, Ksq);
+                        d -= 2 * TPR;
+                        sd -= dstep;
+                        if (sd < 0) sd += R;
                     }
                 }
             if (nn > 0) {
@@ -838,17 +800,166 @@ k_diffusion_rows(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, i
     }
 }
 
-// The wavefront form: rows (k_diffusion_rows, the FP32 default) or task
-// tables (k_diffusion_ring, the FP64 default: the FP64 pipe bounds both and
-// the tables form measured faster there); NUDIM_DIFFUSION=rows|tables
-// selects one.  Both give the same cells bit for bit.  Read at every launch
-// (a captured graph keeps the form it was captured with).
-template <typename T> static bool diffusion_tables()
+// The row form with two rows per thread: rows (2r, 2r + 1) meet a diagonal d
+// at adjacent positions of its slot, so one thread updates both cells of a
+// sweep together: their centres, the W of the first (= N of the second) and
+// the second's W, the first's E and S (= E of the second) and the second's S
+// come from three 8-byte and two 4-byte shared-memory loads instead of ten,
+// the two results go out as one 8-byte store, and the FP32 arithmetic of the
+// pair runs as paired instructions (each the same IEEE operation as
+// diff_cell's, so the results are bit-identical).  A pair whose second row
+// or either cell is off the plane writes that position's old value back (the
+// position belongs to no cell of the diagonal; only this thread writes it).
+// A warp owns 64 rows and one of TPR sweep classes.  Slots are S >= ny + 1
+// values (S even: the pairs' 8-byte accesses stay aligned).  Requires
+// min(ny, nx) <= kDiffPf * blockDim.x, blockDim.x a multiple of 32 TPR and,
+// FP32, blockDim.x <= 768.
+template <typename T, int TPR>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 768 : 1024, sizeof(T) == 4 ? 2 : 1)
+k_diffusion_pairs(T *u, int ny, int nx, int nxb, double lambda_d, double ksq_d, int niter,
+                  int G, int R, int S)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *ring = (T *)smraw;  // R slots of S >= ny + 1 values (S even)
+    T *U = u + (size_t)blockIdx.x * ny * nx;
+    const T lambda = (T)lambda_d, Ksq = (T)ksq_d;
+    const int D = ny + nx - 1, L = min(ny, nx);
+    auto y0 = [&](int d) { return max(0, d - (nx - 1)); };
+    auto len = [&](int d) { return min(d, ny - 1) - y0(d) + 1; };
+    auto slot = [&](int d) { return ring + (size_t)(d % R) * S + y0(d); };
+    auto cell = [&](int d, int i) -> size_t {
+        int a = y0(d);
+        return (size_t)(a + i) * nx + (d - a - i);
+    };
+    using T2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cls = warp % TPR;
+    const int pfirst = (warp / TPR) * 32 + lane, pstride = blockDim.x / TPR;
+    const int dstep = (2 * TPR) % R;
+    const int npairs = (ny + 1) >> 1;
+    for (int s0 = 0; s0 < niter; s0 += G) {
+        const int gc = min(G, niter - s0);
+        const int nsteps = D + 2 * (gc - 1);
+        for (int d = 0; d < 2 && d < D; d++) {
+            T *sd = slot(d);
+            for (int i = threadIdx.x; i < len(d); i += blockDim.x) sd[i] = U[cell(d, i)];
+        }
+        __syncthreads();
+        for (int t = 0; t < nsteps; t++) {
+            const int dn = t + 2;
+            const int nn = dn < D ? len(dn) : 0;
+            const int npf = (L + blockDim.x - 1) / blockDim.x;
+            T pf[kDiffPf];
+#pragma unroll
+            for (int k = 0; k < kDiffPf; k++) {
+                if (k >= npf) break;
+                const int i = threadIdx.x + k * blockDim.x;
+                pf[k] = i < nn ? U[cell(dn, i)] : T(0);
+            }
+            if (cls < gc)
+                for (int pr = pfirst; pr < npairs && 2 * pr <= t; pr += pstride) {
+                    const int y = 2 * pr;  // rows y, y + 1
+                    // sweeps of this class with a cell in row y or y + 1:
+                    // x = t - y - 2g in [0, nx] (row y + 1 has x - 1) and g < gc
+                    const int ghi = min(gc - 1, (t - y) >> 1);
+                    const int over = t - y - nx;  // x <= nx  <=>  g >= over / 2
+                    const int glo = over > 0 ? (over + 1) >> 1 : 0;
+                    int g = glo + ((cls - glo) % TPR + TPR) % TPR;
+                    const bool hasN = y > 0, hasS1 = y + 1 < ny - 1;
+                    const int yN = hasN ? y - 1 : y + 1;  // in-slot when clamped
+                    const int yS = y + 2 < S ? y + 2 : y;
+                    int d = t - 2 * g, sd = d % R;
+                    for (; g <= ghi; g += TPR) {
+                        const int x = d - y;  // row y + 1: x - 1
+                        const int sm = sd == 0 ? R - 1 : sd - 1, sp = sd == R - 1 ? 0 : sd + 1;
+                        T *rc = ring + sd * S;
+                        const T *rm = ring + sm * S, *rp = ring + sp * S;
+                        const T2 c = *reinterpret_cast<const T2 *>(rc + y);
+                        const T2 m = *reinterpret_cast<const T2 *>(rm + y);  // W0 = N1, W1
+                        const T2 q = *reinterpret_cast<const T2 *>(rp + y);  // E0, S0 = E1
+                        const T mN = rm[yN], pS = rp[yS];
+                        // row y: N = rm[y-1], W = rm[y], S = rp[y+1], E = rp[y]
+                        // row y+1: N = rm[y], W = rm[y+1], S = rp[y+2], E = rp[y+1]
+                        const int x1 = x - 1;
+                        T n0 = hasN ? mN : c.x, w0 = x > 0 ? m.x : c.x, s0v = q.y;
+                        T e0 = x == nxb - 1 ? c.x : (x + 1 < nx ? q.x : T(0));
+                        if (y == ny - 1) s0v = c.x;  // last row (odd ny): S clamps to itself
+                        T n1 = m.x, w1 = x1 > 0 ? m.y : c.y, s1 = hasS1 ? pS : c.y;
+                        T e1 = x1 == nxb - 1 ? c.y : (x1 + 1 < nx ? q.y : T(0));
+                        T u0, u1;
+                        if constexpr (sizeof(T) == 4) {
+                            auto f2 = [](float a, float b) { return make_float2(a, b); };
+                            auto sub = [](float2 a, float2 b) {
+                                return __fadd2_rn(a, make_float2(-b.x, -b.y));
+                            };
+                            const float2 cc = f2(c.x, c.y), k2 = f2(Ksq, Ksq);
+                            const float2 gN = sub(f2(n0, n1), cc), gS = sub(f2(s0v, s1), cc),
+                                         gE = sub(f2(e0, e1), cc), gW = sub(f2(w0, w1), cc);
+                            auto coef = [&](float2 gg) {
+                                const float2 dd = __ffma2_rn(gg, gg, k2);
+                                return __fmul2_rn(k2, f2(rcp_approx(dd.x), rcp_approx(dd.y)));
+                            };
+                            float2 sum = __fmul2_rn(coef(gN), gN);
+                            sum = __ffma2_rn(coef(gS), gS, sum);
+                            sum = __ffma2_rn(coef(gE), gE, sum);
+                            sum = __ffma2_rn(coef(gW), gW, sum);
+                            const float2 uu = __ffma2_rn(f2(lambda, lambda), sum, cc);
+                            u0 = uu.x;
+                            u1 = uu.y;
+                        } else {
+                            u0 = diff_cell<T>(c.x, n0, s0v, e0, w0, lambda, Ksq);
+                            u1 = diff_cell<T>(c.y, n1, s1, e1, w1, lambda, Ksq);
+                        }
+                        // a cell off the plane keeps its slot's old value
+                        if (x > nx - 1) u0 = c.x;
+                        if (x1 < 0 || y + 1 >= ny) u1 = c.y;
+                        T2 o;
+                        o.x = u0;
+                        o.y = u1;
+                        *reinterpret_cast<T2 *>(rc + y) = o;
+                        d -= 2 * TPR;
+                        sd -= dstep;
+                        if (sd < 0) sd += R;
+                    }
+                }
+            if (nn > 0) {
+                T *sd = slot(dn);
+#pragma unroll
+                for (int k = 0; k < kDiffPf; k++) {
+                    if (k >= npf) break;
+                    const int i = threadIdx.x + k * blockDim.x;
+                    if (i < nn) sd[i] = pf[k];
+                }
+            }
+            const int df = t - 2 * gc + 1;
+            if (df >= 0 && df < D) {
+                const T *sd = slot(df);
+                for (int i = threadIdx.x; i < len(df); i += blockDim.x) U[cell(df, i)] = sd[i];
+            }
+            __syncthreads();
+        }
+        {
+            const T *sd = slot(D - 1);
+            for (int i = threadIdx.x; i < len(D - 1); i += blockDim.x) U[cell(D - 1, i)] = sd[i];
+        }
+        __syncthreads();
+    }
+}
+
+// The wavefront form: pairs (k_diffusion_pairs, the FP32 default), rows
+// (k_diffusion_rows) or task tables (k_diffusion_ring, the FP64 default: the
+// FP64 pipe bounds every form there and the tables form measured fastest);
+// NUDIM_DIFFUSION=pairs|rows|tables selects one.  All give the same cells bit
+// for bit.  Read at every launch (a captured graph keeps the form it was
+// captured with).
+enum DiffForm { DF_PAIRS, DF_ROWS, DF_TABLES };
+template <typename T> static DiffForm diffusion_form()
 {
     const char *e = getenv("NUDIM_DIFFUSION");
-    if (e && !strcmp(e, "tables")) return true;
-    if (e && !strcmp(e, "rows")) return false;
-    return sizeof(T) == 8;
+    if (e && !strcmp(e, "tables")) return DF_TABLES;
+    if (e && !strcmp(e, "rows")) return DF_ROWS;
+    if (e && !strcmp(e, "pairs")) return DF_PAIRS;
+    return sizeof(T) == 8 ? DF_TABLES : DF_PAIRS;
 }
 
 template <typename T>
@@ -863,14 +974,45 @@ int diffusion_run(T *u, int nz, int ny, int nx, int nx_bound, float lambda, floa
     // up to 160 KB of ring
     bool two = sizeof(T) == 4 && P <= 512;
     const size_t budget = two ? ((size_t)108 << 10) : ((size_t)160 << 10);
-    if (!diffusion_tables<T>()) {
-        // row form: slots of ny values; TPR sweep classes (a power of two)
-        // so that 32-row warps x classes fill 768 threads (FP32, two CTAs per
-        // SM) or 1024 (FP64)
+    const DiffForm form = diffusion_form<T>();
+    const int cap = sizeof(T) == 4 ? 768 : 1024;
+    if (form == DF_PAIRS) {
+        // two rows per thread: slots of S = ny + 1 rounded up to even values;
+        // TPR sweep classes (a power of two) so that 64-row warps x classes
+        // fill up to 768 (FP32, two CTAs per SM) or 1024 threads
+        const int S = (ny + 2) & ~1, Pp = (((ny + 1) >> 1) + 31) & ~31;
+        int G = (int)((budget / (sizeof(T) * (size_t)S) - 2) / 2);
+        if (G > niter) G = niter;
+        if (G > kDiffMaxG) G = kDiffMaxG;
+        int tpr = 1;
+        while (tpr < 8 && 2 * tpr * Pp <= cap && 2 * tpr <= G) tpr *= 2;
+        const int threads = std::min(cap, tpr * Pp);
+        if (G >= 1 && L <= kDiffPf * threads) {
+            const int R = 2 * G + 2;
+            const size_t smem = sizeof(T) * (size_t)R * S;
+#define NUDIM_DIFF_PAIRS(TP)                                                                    \
+    do {                                                                                        \
+        NUDIM_CUDA(cudaFuncSetAttribute(k_diffusion_pairs<T, TP>,                               \
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 160 << 10)); \
+        k_diffusion_pairs<T, TP><<<nz, threads, smem, st>>>(u, ny, nx, nx_bound, (double)lambda, \
+                                                             ksq, niter, G, R, S);              \
+    } while (0)
+            if (tpr == 8) NUDIM_DIFF_PAIRS(8);
+            else if (tpr == 4) NUDIM_DIFF_PAIRS(4);
+            else if (tpr == 2) NUDIM_DIFF_PAIRS(2);
+            else NUDIM_DIFF_PAIRS(1);
+#undef NUDIM_DIFF_PAIRS
+            NUDIM_LAUNCH_CHECK();
+            return NUDIM_OK;
+        }
+    }
+    if (form == DF_ROWS) {
+        // one row per thread: slots of ny values; TPR sweep classes so that
+        // 32-row warps x classes fill up to 768 or 1024 threads
         int G = (int)((budget / (sizeof(T) * (size_t)ny) - 2) / 2);
         if (G > niter) G = niter;
         if (G > kDiffMaxG) G = kDiffMaxG;
-        const int cap = sizeof(T) == 4 ? 768 : 1024, Py = (ny + 31) & ~31;
+        const int Py = (ny + 31) & ~31;
         int tpr = 1;
         while (tpr < 8 && 2 * tpr * Py <= cap && 2 * tpr <= G) tpr *= 2;
         const int threads = std::min(cap, tpr * Py);

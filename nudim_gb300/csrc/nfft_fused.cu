@@ -1207,7 +1207,7 @@ k_colifft_fs(const cplx_t<T> *__restrict__ G, int N0, int n1, const cplx_t<T> *_
 // is reused for the inverse (one barrier between the last read and the first
 // write).  In place: the CTA reads and writes the same N0 x 4 values of H.
 template <typename T, int R1, int R2>
-__global__ void __launch_bounds__(4 * R2)
+__global__ void __launch_bounds__(4 * R2, 3)
 k_col_toeplitz(cplx_t<T> *__restrict__ H, int N0, int n1, const cplx_t<T> *__restrict__ tw0,
                const cplx_t<T> *__restrict__ khat)
 {

@@ -2,8 +2,8 @@
 reference's own denoise.c and against the oracle.  FP64: diffusion is
 bit-identical (no reductions); TV differs only through the order of its two
 global sums (tolerance 1e-12).  FP32: 1e-4.  Diffusion runs in both of its
-wavefront forms (NUDIM_DIFFUSION=rows|tables), which update the same cells
-from the same neighbours and so agree bit for bit; TV runs fused and unfused
+wavefront forms (NUDIM_DIFFUSION=pairs|rows|tables), which update the same
+cells from the same neighbours and so agree bit for bit; TV runs fused and unfused
 (NUDIM_TV=fused|unfused), also bit for bit."""
 import numpy as np
 import pytest
@@ -43,7 +43,7 @@ def test_tv_height_golden(gpu_ctx, nudim_built, golden, n):
     assert rel(out, golden["th_%d_out" % n]) < 1e-12
 
 
-FORMS = ["rows", "tables"]
+FORMS = ["pairs", "rows", "tables"]
 
 
 @pytest.fixture(params=FORMS)
@@ -73,7 +73,7 @@ def test_diffusion_nz_ne_np_vs_oracle(gpu_ctx, orc, nudim_built, shape, nxb, for
 
 
 @pytest.mark.parametrize("shape,nxb,it", [((3, 384, 384), 3, 30), ((2, 100, 300), 2, 70),
-                                          ((2, 300, 100), 2, 70)])
+                                          ((2, 300, 100), 2, 70), ((2, 101, 37), 2, 45)])
 def test_diffusion_forms_agree_at_size(gpu_ctx, orc, nudim_built, monkeypatch, shape, nxb, it):
     """A 384 x 384 plane (the largest configuration's plane, one sweep
     group), and ragged planes with more sweeps than one group holds: FP64
@@ -85,10 +85,11 @@ def test_diffusion_forms_agree_at_size(gpu_ctx, orc, nudim_built, monkeypatch, s
     for f in FORMS:
         monkeypatch.setenv("NUDIM_DIFFUSION", f)
         outs[f] = [run_df(gpu_ctx, nudim_built, v, p, 0.25, 0.005, it, nxb) for p in (0, 1)]
-    assert np.array_equal(outs["rows"][0], orc.diffusion_2d(v, 0.25, 0.005, it, nx_bound=nxb))
-    assert np.array_equal(outs["rows"][0], outs["tables"][0])
-    assert np.array_equal(outs["rows"][1], outs["tables"][1])
-    assert rel(outs["rows"][1], outs["rows"][0]) < 1e-4
+    assert np.array_equal(outs["tables"][0], orc.diffusion_2d(v, 0.25, 0.005, it, nx_bound=nxb))
+    for f in ("pairs", "rows"):
+        assert np.array_equal(outs[f][0], outs["tables"][0]), f
+        assert np.array_equal(outs[f][1], outs["tables"][1]), f
+    assert rel(outs["tables"][1], outs["tables"][0]) < 1e-4
 
 
 def test_tv_fp32_and_large(gpu_ctx, orc, nudim_built):
