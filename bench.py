@@ -23,8 +23,8 @@ host cores), `batched` (48 uneven TV jobs stepped together, one stream
 each), `serving` (Poisson arrivals into the continuous-batching server,
 p50/p99 latency), `cpu_baseline` (the oracle on the host cores: whole
 iterations of the workload's geometry at one Z-plane per thread, and on one
-core), and with --large the 768^2 x 256 TV configuration with its FP64
-correction.
+core), `large` (the 768^2 x 256 TV configuration's mixed form; with
+--large also its FP64 form, FP64 correction and accuracy).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
        [--large] [--batch-jobs J] [--serve-jobs J] [--serve-rate R] [--serve-fp64
@@ -218,11 +218,16 @@ MEASURED_ADJOINT_TRAFFIC_PER_PLANE = ((172.924160e6 + 216.713216e6)    # k_sprea
                                       + (268.486656e6 + 75.897088e6)   # k_colifft_fs
                                       + (100.737792e6 + 36.037120e6)) / 32  # k_rowifft_crop
 # The same for the Toeplitz operator pass (k_rowfft_fs + k_col_toeplitz +
-# k_rowifft_crop_fs in its p^H q mode), 32-plane launches: the 100 MB of row
-# spectra between the passes stay partly in the 129 MB L2 at that size.
-MEASURED_TOEPLITZ_TRAFFIC_PER_PLANE = ((37.8e6 + 36.6e6)      # k_rowfft_fs
-                                       + (109.1e6 + 42.6e6)   # k_col_toeplitz
-                                       + (138.5e6 + 15.6e6)) / 32  # k_rowifft_crop_fs
+# k_rowifft_crop_fs in its p^H q mode) per circulant size, 32-plane launches:
+# the row spectra between the passes stay partly in the 129 MB L2 at that size.
+MEASURED_TOEPLITZ_TRAFFIC_PER_PLANE = {
+    768: ((37.8e6 + 15.6e6)                 # k_rowfft_fs<.., 24, 32>
+          + (80.3e6 + 17.5e6)               # k_col_toeplitz<.., 24, 32>
+          + (113.3e6 + 13.4e6)) / 32,       # k_rowifft_crop_fs<.., 24, 32>
+    1024: ((37.8e6 + 36.6e6)                # k_rowfft_fs
+           + (109.1e6 + 42.6e6)             # k_col_toeplitz
+           + (138.5e6 + 15.6e6)) / 32,      # k_rowifft_crop_fs
+}
 
 
 def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):
@@ -231,9 +236,9 @@ def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):
     - The Toeplitz operator pass of the CGNR (k_rowfft_fs + k_col_toeplitz +
       k_rowifft_crop_fs, class "toeplitz"): 11 per Z-plane and outer
       iteration (one before the loop, one per step).  Unit: one Z-plane's
-      pass, c (3 P^2 + 4 P n) bytes -- p in, T p out and p read again for
-      p^H T p, and the P x n row spectra written, read and written by the
-      column pass, and read back.
+      pass, c (3 P^2 + 4 P nt) bytes -- p in, T p out and p read again for
+      p^H T p, and the P x nt row spectra written, read and written by the
+      column pass, and read back (nt: the circulant's size, 768 for P = 384).
     - The adjoint NFFT (k_spread_gather + k_spread_fixup + k_colifft_fs +
       k_rowifft_crop_fs, classes "spread" + "crop"): 11 per Z-plane and outer
       iteration with the NFFT form of the CGNR, 1 with the Toeplitz form.
@@ -250,8 +255,10 @@ def roofline_from_profile(prof, peak_gbs, peak_kind, r, csize, steps):
     if toep[1] > 0:
         units = 11 * nz * steps
         launches = toep[1] / 3.0  # three passes per launch of the group
-        unit = csize * (3 * P * P + 4 * P * n)
-        tr = MEASURED_TOEPLITZ_TRAFFIC_PER_PLANE
+        # the circulant: 768 points when 2P - 1 <= 768 < n, else n
+        nt = 768 if (2 * P - 1 <= 768 < n and os.environ.get("NUDIM_TOEPLITZ_GRID") != "nfft") else n
+        unit = csize * (3 * P * P + 4 * P * nt)
+        tr = MEASURED_TOEPLITZ_TRAFFIC_PER_PLANE.get(nt)
         groups.append(("Toeplitz operator pass",
                        "Toeplitz operator pass (k_rowfft_fs + k_col_toeplitz + k_rowifft_crop_fs)",
                        toep[0], units, launches, unit, tr))
@@ -594,6 +601,35 @@ def fp64_peak():
         return None
 
 
+def large_quick(ctx, steps=3, warmup=2):
+    """The large-volume configuration's mixed form alone (512 x 512 x 256
+    blob + shell phantom, 121 tilts, np = nx = 768, nz = 256, --weight, TV):
+    `steps` iterations after `warmup`, CUDA events on the job's stream.  The
+    default bench line carries it; --large adds the FP64 form, the FP64
+    correction and the accuracy comparison."""
+    import nudim_gb300 as ng
+    from nudim_gb300.synth import CONFIGS, MASTER_SEED, make_inputs
+    r = dict(CONFIGS["cfg5"]["recon"])
+    vol, proj = make_inputs(ctx, "cfg5", seed=MASTER_SEED)
+    del vol
+    V = r["nz"] * r["np"] ** 2
+    t0 = time.perf_counter()
+    job = ng.Job(ctx, **job_kwargs(r, ng.MIXED))
+    job.set_projections(proj)
+    job.sync()
+    t_setup = time.perf_counter() - t0
+    job.step(warmup)
+    ms = timed_steps(ctx, job, steps)
+    job.close()
+    out = {"value": V * steps / (ms / 1e3), "unit": "voxel-iters/s", "steps": steps,
+           "warmup": warmup, "ms_per_step": ms / steps, "setup_s": t_setup,
+           "config": {"workload": "512x512x256 blob+shell phantom, 121 tilts -60..60 step 1, "
+                                  "SNR 0.3, np=nx=768, nz=256, padangle 1, --weight, TV, "
+                                  "mixed form", "voxels": V}}
+    log("large (mixed): %.1f ms/iteration, %.3e voxel-iters/s" % (ms / steps, out["value"]))
+    return out
+
+
 def large_bench(ctx, steps=10, warmup=3):
     """The large-volume configuration: 512 x 512 x 256 blob + shell phantom,
     121 tilts (-60..60 step 1) at SNR 0.3, reconstructed at np = nx = 768,
@@ -871,6 +907,8 @@ def run_ours(args):
                                       "over_fp64": (ms64 / fp64_steps) / t_sched}
     if args.large:
         line["large"] = large_bench(ctx)
+    elif not args.no_large_quick:
+        line["large"] = large_quick(ctx)
     if args.batch_jobs > 0:
         line["batched"] = {"mixed": batched_bench(ctx, args.batch_jobs, args.steps, args.warmup,
                                                   ng.MIXED)}
@@ -952,7 +990,11 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--large", action="store_true",
-                    help="also run the large-volume configuration (768^2 x 256, ~3 min)")
+                    help="the large-volume configuration with the FP64 form, the FP64 "
+                         "correction and the accuracy comparison (~3 min) instead of its "
+                         "mixed-form timing alone")
+    ap.add_argument("--no-large-quick", action="store_true",
+                    help="skip the large-volume configuration's mixed-form timing")
     ap.add_argument("--batch-jobs", type=int, default=48,
                     help="jobs in the batched measurement (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=24,

@@ -210,6 +210,10 @@ template <typename T> struct NfftDev {
     C *khat = nullptr;
     T *ones = nullptr;
     bool toeplitz = false;
+    // the circulant's size: 768 (= 24 x 32) when 2 N - 1 <= 768 < n, else the
+    // NFFT grid n; twT: its twiddles e^{-2 pi i k / nT}
+    int nT = 0;
+    C *twT = nullptr;
     bool toeplitz_fits() const
     {
         return fused && row_fs && N0 == N1 && n0 == n1 && (n0 == 256 || n0 == 512 || n0 == 1024);

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <type_traits>
 
 #include "engine.cuh"
@@ -232,11 +233,37 @@ template <typename T, int DIR> __device__ __forceinline__ cplx_t<T> w32(int p)
     return mkc<T>((T)cs, (T)(DIR * sn));
 }
 
-// R-point DFT (R = 16 or 32) of a[0..R) in registers; X[p] is left in
-// a[fs_out<R>(p)].
+// W_24^p = e^{DIR 2 pi i p / 24}, p = 0..23
+template <typename T, int DIR> __device__ __forceinline__ cplx_t<T> w24(int p)
+{
+    // cos(2 pi q / 24), q = 0..6
+    constexpr double c[7] = {1.0,
+                             0.96592582628906828675,
+                             0.86602540378443864676,
+                             0.70710678118654752440,
+                             0.5,
+                             0.25881904510252076235,
+                             0.0};
+    const int q = p % 6, h = p / 6;  // p = 6h + q: rotate by h quarter turns
+    double cs, sn;
+    const double cq = c[q], sq = c[6 - q];
+    switch (h & 3) {
+    case 0: cs = cq; sn = sq; break;
+    case 1: cs = -sq; sn = cq; break;
+    case 2: cs = -cq; sn = -sq; break;
+    default: cs = sq; sn = -cq; break;
+    }
+    return mkc<T>((T)cs, (T)(DIR * sn));
+}
+
+// R-point DFT (R = 16, 24 or 32) of a[0..R) in registers; X[p] is left in
+// a[fs_out<R>(p)].  R = 24: three 8-point DFTs over a[3u + v], the twiddles
+// W_24^{v p8} and 3-point DFTs over v, X[p8 + 8q] in a[3 p8 + q].
 template <int R> __device__ __forceinline__ constexpr int fs_out(int p)
 {
-    return R == 16 ? dft_out<16>(p) : (p < 16 ? 2 * dft_out<16>(p) : 2 * dft_out<16>(p - 16) + 1);
+    return R == 16   ? dft_out<16>(p)
+           : R == 24 ? 3 * (p & 7) + (p >> 3)
+                     : (p < 16 ? 2 * dft_out<16>(p) : 2 * dft_out<16>(p - 16) + 1);
 }
 
 template <typename T, int DIR, int R> __device__ __forceinline__ void fs_dft(cplx_t<T> *a)
@@ -244,6 +271,32 @@ template <typename T, int DIR, int R> __device__ __forceinline__ void fs_dft(cpl
     using C = cplx_t<T>;
     if constexpr (R == 16) {
         dft_regs<T, DIR, 16>(a);
+    } else if constexpr (R == 24) {
+        C e[3][8];
+#pragma unroll
+        for (int v = 0; v < 3; v++)
+#pragma unroll
+            for (int u = 0; u < 8; u++) e[v][u] = a[3 * u + v];
+#pragma unroll
+        for (int v = 0; v < 3; v++) dft_regs<T, DIR, 8>(e[v]);
+        // X[p8 + 8q] = sum_v (W_24^{v p8} E_v[p8]) W_3^{v q}
+        const T h3 = (T)0.86602540378443864676;  // sqrt(3) / 2
+#pragma unroll
+        for (int p8 = 0; p8 < 8; p8++) {
+            const C x0 = e[0][dft_out<8>(p8)];
+            C x1 = e[1][dft_out<8>(p8)], x2 = e[2][dft_out<8>(p8)];
+            if (p8) {
+                x1 = cmul<T>(x1, w24<T, DIR>(p8));
+                x2 = cmul<T>(x2, w24<T, DIR>(2 * p8));
+            }
+            const C sm = mkc<T>(x1.x + x2.x, x1.y + x2.y), df = mkc<T>(x1.x - x2.x, x1.y - x2.y);
+            const C mid = mkc<T>(x0.x - (T)0.5 * sm.x, x0.y - (T)0.5 * sm.y);
+            // DIR i (sqrt(3)/2) (x1 - x2)
+            const C rot = mkc<T>(-(T)DIR * h3 * df.y, (T)DIR * h3 * df.x);
+            a[3 * p8] = mkc<T>(x0.x + sm.x, x0.y + sm.y);
+            a[3 * p8 + 1] = mkc<T>(mid.x + rot.x, mid.y + rot.y);
+            a[3 * p8 + 2] = mkc<T>(mid.x - rot.x, mid.y - rot.y);
+        }
     } else {
         C e[16], o[16];
 #pragma unroll
@@ -1096,7 +1149,8 @@ k_rowifft_crop_fs(const cplx_t<T> *__restrict__ Hp, int N0, int N1, const T *__r
 #pragma unroll
             for (int k2 = 0; k2 < R2; k2++) {
                 // output index l1 = k1 + R1 k2 is column c = l1 + N1/2 (mod n1)
-                const int c = (k1 + R1 * k2 + N1 / 2) & (n1 - 1);
+                int c = k1 + R1 * k2 + N1 / 2;
+                if (c >= n1) c -= n1;
                 if (c < N1) {
                     const C g = y[fs_out<R2>(k2)];
                     const size_t o = (size_t)gb * ca.out_stride + (size_t)a * N1 + c;
@@ -1212,7 +1266,7 @@ k_col_toeplitz(cplx_t<T> *__restrict__ H, int N0, int n1, const cplx_t<T> *__res
                const cplx_t<T> *__restrict__ khat)
 {
     using C = cplx_t<T>;
-    constexpr int n0 = R1 * R2, BC = 4, CS = fs_col_stride<R1, R2>(), KI = R1 / R2;
+    constexpr int n0 = R1 * R2, BC = 4, CS = fs_col_stride<R1, R2>(), KI = (R1 + R2 - 1) / R2;
     static_assert(R2 * (R1 + 1) <= CS, "inverse exchange exceeds the column stride");
     extern __shared__ __align__(16) unsigned char smraw[];
     C *S = (C *)smraw;
@@ -1240,12 +1294,14 @@ k_col_toeplitz(cplx_t<T> *__restrict__ H, int N0, int n1, const cplx_t<T> *__res
     C y[KI][R2];
 #pragma unroll
     for (int i = 0; i < KI; i++)
+        if (j + R2 * i < R1)
 #pragma unroll
-        for (int jj = 0; jj < R2; jj++) y[i][jj] = S[c * CS + (j + R2 * i) * (R2 + 1) + jj];
+            for (int jj = 0; jj < R2; jj++) y[i][jj] = S[c * CS + (j + R2 * i) * (R2 + 1) + jj];
     __syncthreads();  // S is reused for the inverse exchange
 #pragma unroll
     for (int i = 0; i < KI; i++) {
         const int k1 = j + R2 * i;
+        if (k1 >= R1) break;
         fs_dft<T, -1, R2>(y[i]);
         C z[R2];
         const C *kp = khat + (((size_t)cb * R2) * R1 + k1) * BC + c;
@@ -1273,7 +1329,8 @@ k_col_toeplitz(cplx_t<T> *__restrict__ H, int N0, int n1, const cplx_t<T> *__res
         fs_dft<T, +1, R1>(w);
 #pragma unroll
         for (int t1 = 0; t1 < R1; t1++) {
-            const int a = (t2 + R2 * t1 + N0 / 2) & (n0 - 1);
+            int a = t2 + R2 * t1 + N0 / 2;
+            if (a >= n0) a -= n0;
             if (a < N0) Hb[(size_t)a * n1] = w[fs_out<R1>(t1)];
         }
     }
@@ -1294,7 +1351,7 @@ __global__ void k_toep_embed(const cplx_t<T> *__restrict__ Kq, int N0, int N1, i
     const int m0 = a - N0 / 2 + ((q >> 1) ? N0 / 2 : -N0 / 2);
     const int m1 = cc - N1 / 2 + ((q & 1) ? N1 / 2 : -N1 / 2);
     if (m0 <= -N0 || m0 >= N0 || m1 <= -N1 || m1 >= N1) return;
-    circ[(size_t)(m0 & (n0 - 1)) * n1 + (m1 & (n1 - 1))] = Kq[i];
+    circ[(size_t)(m0 < 0 ? m0 + n0 : m0) * n1 + (m1 < 0 ? m1 + n1 : m1)] = Kq[i];
 }
 
 // The circulant's DFT (row-major n0 x n1) divided by n0 n1, in the order
@@ -1620,6 +1677,23 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     NUDIM_CUDA(cudaFuncSetAttribute(k_col_toeplitz<T, 16, 16>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)(sizeof(C) * 4 * fs_col_stride<16, 16>())));
+    NUDIM_CUDA(cudaFuncSetAttribute(k_col_toeplitz<T, 24, 32>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(C) * 4 * fs_col_stride<24, 32>())));
+    {
+        // the 768-point circulant's row passes (24 x 32)
+        const int lt = (int)(sizeof(C) * 4 * fs_row_stride<24, 32>());
+        NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft_fs<T, PM_COMPLEX, 24, 32>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, lt));
+        NUDIM_CUDA(cudaFuncSetAttribute(k_rowfft_fs<T, PM_REAL_INIT, 24, 32>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, lt));
+        NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_PLAIN, 24, 32>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, lt));
+        NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_TRESID, 24, 32>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, lt));
+        NUDIM_CUDA(cudaFuncSetAttribute(k_rowifft_crop_fs<T, CM_TPDOT, 24, 32>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, lt));
+    }
     NUDIM_CUDA(cudaFuncSetAttribute(k_colifft_fs<T, 32, 32>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)(sizeof(C) * 4 * fs_col_stride<32, 32>())));
@@ -1647,6 +1721,9 @@ template <typename T> void NfftDev<T>::release_fused()
 {
     void *ptrs[] = {tw0,    tw1,  blk_off, ent,  nslots, band_off, band_node,
                     units,  band_w, e_rb, e_cc, e_qa, e_q1, fixups, khat, ones};
+    if (twT && twT != tw0) cudaFreeAsync(twT, ast);
+    twT = nullptr;
+    nT = 0;
     khat = nullptr;
     ones = nullptr;
     toeplitz = false;
@@ -1965,7 +2042,12 @@ template <typename T> int NfftDev<T>::toeplitz_init(const double *x, const T *w,
     }
     if (toeplitz) return NUDIM_OK;
     const double two_pi = 6.283185307179586;
-    const size_t N = (size_t)N0 * N1, nn = (size_t)n0 * n1;
+    // the smallest supported circulant that holds |m| < N without wrap
+    // (NUDIM_TOEPLITZ_GRID=nfft keeps the NFFT grid's size)
+    const char *eg = getenv("NUDIM_TOEPLITZ_GRID");
+    const bool small = !(eg && !strcmp(eg, "nfft"));
+    const int nt = (small && 2 * N0 - 1 <= 768 && n0 > 768) ? 768 : n0;
+    const size_t N = (size_t)N0 * N1, nn = (size_t)nt * nt;
     std::vector<C> hv(4 * (size_t)M);
     for (int q = 0; q < 4; q++) {
         const double s0 = (q >> 1) ? N0 / 2 : -N0 / 2, s1 = (q & 1) ? N1 / 2 : -N1 / 2;
@@ -1977,7 +2059,12 @@ template <typename T> int NfftDev<T>::toeplitz_init(const double *x, const T *w,
         }
     }
     std::vector<T> hones(std::max(N0, N1), T(1));
-    void *dv = nullptr, *dk = nullptr, *dc = nullptr, *d1 = nullptr, *kh = nullptr;
+    std::vector<C> htw(nt);
+    for (int k = 0; k < nt; k++) {
+        const double a = -two_pi * (double)k / nt;
+        htw[k] = mkc<T>((T)std::cos(a), (T)std::sin(a));
+    }
+    void *dv = nullptr, *dk = nullptr, *dc = nullptr, *d1 = nullptr, *kh = nullptr, *dtw = nullptr;
     // temporaries released stream-ordered after their last use; on failure
     // the kept buffers too
     auto done = [&](int e) {
@@ -1986,11 +2073,13 @@ template <typename T> int NfftDev<T>::toeplitz_init(const double *x, const T *w,
         if (e) {
             if (d1) cudaFreeAsync(d1, st);
             if (kh) cudaFreeAsync(kh, st);
+            if (dtw) cudaFreeAsync(dtw, st);
         }
         return e;
     };
     int rc = upload_async(&dv, hv.data(), sizeof(C) * hv.size(), st);
     if (!rc) rc = upload_async(&d1, hones.data(), sizeof(T) * hones.size(), st);
+    if (!rc && nt != n0) rc = upload_async(&dtw, htw.data(), sizeof(C) * htw.size(), st);
     if (rc) return done(rc);
     if (cudaMallocAsync(&dk, sizeof(C) * 4 * N, st) != cudaSuccess ||
         cudaMallocAsync(&dc, sizeof(C) * nn, st) != cudaSuccess ||
@@ -2012,18 +2101,18 @@ template <typename T> int NfftDev<T>::toeplitz_init(const double *x, const T *w,
         return done(NUDIM_ECUDA);
     }
     k_toep_embed<T><<<(unsigned)ceil_div((long)(4 * N), 256), 256, 0, st>>>(
-        (const C *)dk, N0, N1, n0, n1, (C *)dc);
+        (const C *)dk, N0, N1, nt, nt, (C *)dc);
     ++g_launches;
     cufftHandle h;
-    if ((rc = ctx_fft2d(ctx, n0, n1, 1, prec_of<T>(), &h))) return done(rc);
+    if ((rc = ctx_fft2d(ctx, nt, nt, 1, prec_of<T>(), &h))) return done(rc);
     if (cufftSetStream(h, st) != CUFFT_SUCCESS) {
         set_error("Toeplitz operator: cufftSetStream failed");
         return done(NUDIM_ECUDA);
     }
     if ((rc = fft_exec<T>(h, (C *)dc, CUFFT_FORWARD))) return done(rc);
-    // the column pass's four-step split of n0
-    const int R1 = n0 == 256 ? 16 : 32, R2 = n0 / R1;
-    k_toep_layout<T><<<(unsigned)ceil_div((long)nn, 256), 256, 0, st>>>((const C *)dc, n0, n1, R1,
+    // the column pass's four-step split of the circulant's size
+    const int R1 = nt == 256 ? 16 : nt == 768 ? 24 : 32, R2 = nt / R1;
+    k_toep_layout<T><<<(unsigned)ceil_div((long)nn, 256), 256, 0, st>>>((const C *)dc, nt, nt, R1,
                                                                          R2, (C *)kh);
     ++g_launches;
     if (cudaGetLastError() != cudaSuccess) {
@@ -2033,7 +2122,9 @@ template <typename T> int NfftDev<T>::toeplitz_init(const double *x, const T *w,
     done(NUDIM_OK);
     khat = (C *)kh;
     ones = (T *)d1;
-    bytes += sizeof(C) * nn + sizeof(T) * hones.size();
+    nT = nt;
+    twT = dtw ? (C *)dtw : tw0;
+    bytes += sizeof(C) * nn + sizeof(T) * hones.size() + (dtw ? sizeof(C) * nt : 0);
     toeplitz = true;
     return NUDIM_OK;
 }
@@ -2049,31 +2140,38 @@ int NfftDev<T>::toeplitz_apply(int nplanes, const PadArgs<T> &pa, const CropArgs
         set_error("Toeplitz operator not initialised");
         return NUDIM_ESTATE;
     }
-    int chunk = fused_chunk(nplanes, (size_t)N0 * n1);
+    const int nt = nT;
+    int chunk = fused_chunk(nplanes, (size_t)N0 * nt);
     void *wsv;
-    size_t nH = (size_t)N0 * n1 * chunk;
+    size_t nH = (size_t)N0 * nt * chunk;
     NUDIM_TRY(workspace(sizeof(C) * nH, &wsv));
     C *H = (C *)wsv;
     const double c = sizeof(C);
-    const size_t smem_t = sizeof(C) * 4 *
-                          (n0 == 1024 ? fs_col_stride<32, 32>() : n0 == 512 ? fs_col_stride<32, 16>()
-                                                                            : fs_col_stride<16, 16>());
+    const size_t smem_t =
+        sizeof(C) * 4 *
+        (nt == 1024  ? fs_col_stride<32, 32>()
+         : nt == 768 ? fs_col_stride<24, 32>()
+         : nt == 512 ? fs_col_stride<32, 16>()
+                     : fs_col_stride<16, 16>());
+    const size_t smem_r = nt == 768 ? sizeof(C) * 4 * fs_row_stride<24, 32>() : smem_row;
+    const int trows = nt == 768 ? 4 : rows;
     for (int p0 = 0; p0 < nplanes; p0 += chunk) {
         int nb = std::min(chunk, nplanes - p0);
         {
-            ProfScope ps(ctx, PK_TOEPLITZ, st, nb * c * ((double)N0 * N1 + (double)N0 * n1));
-            dim3 g(ceil_div(N0, rows), nb);
+            ProfScope ps(ctx, PK_TOEPLITZ, st, nb * c * ((double)N0 * N1 + (double)N0 * nt));
+            dim3 g(ceil_div(N0, trows), nb);
 #define NUDIM_TROW(MD, R1, R2)                                                                   \
-    k_rowfft_fs<T, MD, R1, R2><<<g, 128, smem_row, st>>>(pa.src, pa.src_stride, N0, N1, ones,    \
-                                                          ones, tw1, p0, H, pa.f_init,          \
-                                                          pa.f_stride)
+    k_rowfft_fs<T, MD, R1, R2><<<g, 128, smem_r, st>>>(pa.src, pa.src_stride, N0, N1, ones, ones, \
+                                                        twT, p0, H, pa.f_init, pa.f_stride)
             if (pa.mode == PM_COMPLEX) {
-                if (n1 == 1024) NUDIM_TROW(PM_COMPLEX, 32, 32);
-                else if (n1 == 512) NUDIM_TROW(PM_COMPLEX, 32, 16);
+                if (nt == 1024) NUDIM_TROW(PM_COMPLEX, 32, 32);
+                else if (nt == 768) NUDIM_TROW(PM_COMPLEX, 24, 32);
+                else if (nt == 512) NUDIM_TROW(PM_COMPLEX, 32, 16);
                 else NUDIM_TROW(PM_COMPLEX, 16, 16);
             } else {
-                if (n1 == 1024) NUDIM_TROW(PM_REAL_INIT, 32, 32);
-                else if (n1 == 512) NUDIM_TROW(PM_REAL_INIT, 32, 16);
+                if (nt == 1024) NUDIM_TROW(PM_REAL_INIT, 32, 32);
+                else if (nt == 768) NUDIM_TROW(PM_REAL_INIT, 24, 32);
+                else if (nt == 512) NUDIM_TROW(PM_REAL_INIT, 32, 16);
                 else NUDIM_TROW(PM_REAL_INIT, 16, 16);
             }
 #undef NUDIM_TROW
@@ -2081,27 +2179,31 @@ int NfftDev<T>::toeplitz_apply(int nplanes, const PadArgs<T> &pa, const CropArgs
         }
         {
             // H read and written in place; khat (n0 n1 values) read per plane
-            ProfScope ps(ctx, PK_TOEPLITZ, st, nb * c * 2.0 * N0 * n1 + c * (double)n0 * n1);
-            if (n0 == 1024)
-                k_col_toeplitz<T, 32, 32><<<dim3(n1 / 4, nb), 128, smem_t, st>>>(H, N0, n1, tw0,
+            ProfScope ps(ctx, PK_TOEPLITZ, st, nb * c * 2.0 * N0 * nt + c * (double)nt * nt);
+            if (nt == 1024)
+                k_col_toeplitz<T, 32, 32><<<dim3(nt / 4, nb), 128, smem_t, st>>>(H, N0, nt, twT,
                                                                                   khat);
-            else if (n0 == 512)
-                k_col_toeplitz<T, 32, 16><<<dim3(n1 / 4, nb), 64, smem_t, st>>>(H, N0, n1, tw0,
+            else if (nt == 768)
+                k_col_toeplitz<T, 24, 32><<<dim3(nt / 4, nb), 128, smem_t, st>>>(H, N0, nt, twT,
+                                                                                  khat);
+            else if (nt == 512)
+                k_col_toeplitz<T, 32, 16><<<dim3(nt / 4, nb), 64, smem_t, st>>>(H, N0, nt, twT,
                                                                                  khat);
             else
-                k_col_toeplitz<T, 16, 16><<<dim3(n1 / 4, nb), 64, smem_t, st>>>(H, N0, n1, tw0,
+                k_col_toeplitz<T, 16, 16><<<dim3(nt / 4, nb), 64, smem_t, st>>>(H, N0, nt, twT,
                                                                                  khat);
             NUDIM_LAUNCH_CHECK();
         }
         {
-            ProfScope ps(ctx, PK_TOEPLITZ, st, nb * c * ((double)N0 * n1 + 2.0 * N0 * N1));
-            dim3 g(ceil_div(N0, rows), nb);
+            ProfScope ps(ctx, PK_TOEPLITZ, st, nb * c * ((double)N0 * nt + 2.0 * N0 * N1));
+            dim3 g(ceil_div(N0, trows), nb);
 #define NUDIM_TCROP(MD, R1, R2)                                                                  \
-    k_rowifft_crop_fs<T, MD, R1, R2><<<g, 128, smem_row, st>>>(H, N0, N1, ones, ones, tw1, p0, ca)
+    k_rowifft_crop_fs<T, MD, R1, R2><<<g, 128, smem_r, st>>>(H, N0, N1, ones, ones, twT, p0, ca)
 #define NUDIM_TCROP_N(MD)                                                                        \
     do {                                                                                        \
-        if (n1 == 1024) NUDIM_TCROP(MD, 32, 32);                                                \
-        else if (n1 == 512) NUDIM_TCROP(MD, 32, 16);                                            \
+        if (nt == 1024) NUDIM_TCROP(MD, 32, 32);                                                \
+        else if (nt == 768) NUDIM_TCROP(MD, 24, 32);                                            \
+        else if (nt == 512) NUDIM_TCROP(MD, 32, 16);                                            \
         else NUDIM_TCROP(MD, 16, 16);                                                           \
     } while (0)
             if (ca.mode == CM_TRESID) NUDIM_TCROP_N(CM_TRESID);

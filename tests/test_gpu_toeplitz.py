@@ -44,6 +44,35 @@ def run(ctx, nudim_built, monkeypatch, proj, form, **kw):
     return out
 
 
+# np = 320: the 1024-point NFFT grid, the operator on a 768-point circulant
+# (2 np - 1 <= 768: the 24 x 32 four-step FFTs)
+CASE768 = dict(nx=256, nz=8, np=320, gam_min=-60, gam_max=60, interval=3, padangle=1, nhio=0,
+               ner=2, denoise=2, weight=1)
+
+
+def inputs768(orc):
+    vol = small_phantom(256, 8, 12)
+    proj = orc.project_2d1d(vol, 256, -60, 60, 3)
+    rng = np.random.default_rng(12)
+    return proj + 0.05 * proj.std() * rng.standard_normal(proj.shape)
+
+
+def test_toeplitz_cg_768_circulant_fp64(gpu_ctx, orc, nudim_built, monkeypatch):
+    proj = inputs768(orc)
+    kw = dict(CASE768, precision=0)
+    vn, rn, v0n = run(gpu_ctx, nudim_built, monkeypatch, proj, "nfft", **kw)
+    vt, rt, v0t = run(gpu_ctx, nudim_built, monkeypatch, proj, "toeplitz", **kw)
+    print("FP64 Toeplitz (768-point circulant) vs NFFT CGNR: initial %.2e, after 2 ER %.2e"
+          % (rel(v0t, v0n), rel(vt, vn)))
+    assert rel(v0t, v0n) < 1e-8
+    assert rel(vt, vn) < 1e-8
+    assert np.allclose(rt, rn, rtol=1e-8, atol=0)
+    # and the FP32 form on the same circulant
+    v32, r32, v032 = run(gpu_ctx, nudim_built, monkeypatch, proj, "toeplitz", **dict(CASE768, precision=1))
+    print("  FP32 Toeplitz vs FP64 NFFT: initial %.2e, after 2 ER %.2e" % (rel(v032, v0n), rel(v32, vn)))
+    assert rel(v032, v0n) < 1e-4 and rel(v32, vn) < 1e-4
+
+
 @pytest.mark.parametrize("weight", [1, 0])
 def test_toeplitz_cg_matches_nfft_cg_fp64(gpu_ctx, orc, nudim_built, monkeypatch, weight):
     proj = inputs(orc)
