@@ -149,7 +149,6 @@ struct nudim_job {
     int A = 0, M = 0, nmeas = 0, n_unk_row = 0;
     double pad_min = 0, pad_max = 0;
     NfftTables tabs;
-    std::vector<double> x;  // the M polar nodes (x[2j], x[2j+1])
     std::vector<int> known, order, unk_rank;
     std::vector<double> fill;
     bool fill_set = false, ready = false;
@@ -261,10 +260,26 @@ template <typename T> static int state_init(nudim_job *jb, JobState<T> &s)
                                    jb->stream));
     }
     if (use_toeplitz<T>(s.pl)) {
-        // CGNR's normal operator by Toeplitz embedding: T p into q
+        // CGNR's normal operator by Toeplitz embedding: T p into q; its kernel
+        // from the polar set's factors and the radial weights (the same for
+        // every line), in FP64
         NUDIM_TRY(s.alloc(&s.q, V));
-        NUDIM_TRY(s.pl.toeplitz_init(jb->x.data(), s.w, jb->stream));
-        s.bytes += (size_t)s.pl.n0 * s.pl.n1 * sizeof(cplx_t<T>);
+        std::vector<double> r(np), sg(jb->A), cg(jb->A), wall, wr;
+        polar_factors(jb->pad_min, jb->pad_max, jb->d.padangle, np, r.data(), sg.data(),
+                      cg.data());
+        if (jb->d.weight) {
+            wall.resize((size_t)M);
+            cgnr_weights(jb->A, np, jb->d.padangle, wall.data());
+            wr.assign(wall.begin(), wall.begin() + np);
+        }
+        PolarGeom g;
+        g.A = jb->A;
+        g.r = r.data();
+        g.sg = sg.data();
+        g.cg = cg.data();
+        g.wr = jb->d.weight ? wr.data() : nullptr;
+        NUDIM_TRY(s.pl.toeplitz_init(g, jb->stream));
+        s.bytes += (size_t)s.pl.nT * s.pl.nT * sizeof(cplx_t<T>);
     }
     if (jb->d.denoise == NUDIM_DENOISE_TV) {
         NUDIM_TRY(s.alloc(&s.grad, V));
@@ -838,8 +853,7 @@ int nudim_job_create(nudim_ctx *ctx, const nudim_job_desc *desc, nudim_job **out
     jb->nmeas = (int)((d.gam_max - d.gam_min) / d.interval + 0.5) + 1;
     jb->A = polar_lines(d.gam_min, d.interval, d.padangle, &jb->pad_min, &jb->pad_max);
     jb->M = jb->A * d.np;
-    std::vector<double> &x = jb->x;
-    x.resize((size_t)jb->M * 2);
+    std::vector<double> x((size_t)jb->M * 2);
     equal_angle_sample_2d(jb->pad_min, jb->pad_max, d.padangle, d.np, x.data());
     if (build_nfft_tables(d.np, d.np, jb->M, x.data(), 16, 16, &jb->tabs) != 0) {
         set_error("invalid NFFT geometry");

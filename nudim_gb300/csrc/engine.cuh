@@ -155,6 +155,14 @@ template <typename T> struct CropArgs {
     int part_stride = 0;
 };
 
+// The polar node set in factored form for the Toeplitz operator (host
+// arrays): node a * N1 + i = r[i] (sg[a], cg[a]), weight wr[i] (nullptr:
+// unweighted).
+struct PolarGeom {
+    int A = 0;
+    const double *r = nullptr, *sg = nullptr, *cg = nullptr, *wr = nullptr;
+};
+
 // ------------------------------------------------------------ NFFT plan
 template <typename T> struct NfftDev {
     using C = cplx_t<T>;
@@ -204,8 +212,9 @@ template <typename T> struct NfftDev {
     int adjoint(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca, cudaStream_t st);
 
     // CGNR's normal operator A^H W A by Toeplitz embedding (nfft_fused.cu):
-    // khat = the n0 x n1 DFT of its kernel K[m] = sum_j w_j e^{2 pi i m x_j},
-    // |m| < N, divided by n0 n1 and laid out in the column pass's read order;
+    // khat = the nT x nT DFT of its kernel K[m] = sum_j w_j e^{2 pi i m x_j},
+    // |m| < N (computed in FP64), divided by nT^2 and laid out in the column
+    // pass's read order;
     // ones: N0 (or N1, the larger) unit deconvolution factors for the row passes
     C *khat = nullptr;
     T *ones = nullptr;
@@ -218,9 +227,7 @@ template <typename T> struct NfftDev {
     {
         return fused && row_fs && N0 == N1 && n0 == n1 && (n0 == 256 || n0 == 512 || n0 == 1024);
     }
-    // x: the M nodes (host, x[2j], x[2j+1]); w: the CGNR weights (device,
-    // nullptr: unweighted)
-    int toeplitz_init(const double *x, const T *w, cudaStream_t st);
+    int toeplitz_init(const PolarGeom &g, cudaStream_t st);
     // out = T src for nplanes planes of N0 x N1 (the row pass in ca's mode;
     // pa as for trafo: PM_COMPLEX or PM_REAL_INIT)
     int toeplitz_apply(int nplanes, const PadArgs<T> &pa, const CropArgs<T> &ca, cudaStream_t st);

@@ -1260,6 +1260,9 @@ k_colifft_fs(const cplx_t<T> *__restrict__ G, int N0, int n1, const cplx_t<T> *_
 // with the R1-point DFT over k1 (output row t2 + R2 t1).  The exchange buffer
 // is reused for the inverse (one barrier between the last read and the first
 // write).  In place: the CTA reads and writes the same N0 x 4 values of H.
+// Three CTAs per SM (168 registers; capping the 768-point form at 128
+// registers for a fourth CTA made the passes slower, 14.4 -> 16.5 ms per
+// cfg2 iteration).
 template <typename T, int R1, int R2>
 __global__ void __launch_bounds__(4 * R2, 3)
 k_col_toeplitz(cplx_t<T> *__restrict__ H, int N0, int n1, const cplx_t<T> *__restrict__ tw0,
@@ -1336,38 +1339,86 @@ k_col_toeplitz(cplx_t<T> *__restrict__ H, int N0, int n1, const cplx_t<T> *__res
     }
 }
 
-// The kernel's four N0 x N1 quadrants K[k + s_q] (s_q = (+-N0/2, +-N1/2),
-// quadrant q = 2 (s0 > 0) + (s1 > 0), k in [-N/2, N/2)) into the n0 x n1
-// circulant c[m mod n] for |m| < N (zero elsewhere: c is zeroed first).
-template <typename T>
-__global__ void k_toep_embed(const cplx_t<T> *__restrict__ Kq, int N0, int N1, int n0, int n1,
-                             cplx_t<T> *__restrict__ circ)
+// The operator's kernel in FP64 from the polar set's factored form: node
+// (a, i) = r_i (sg_a, cg_a) and weight w_i, so K[m] = sum_a G(m0 sg_a + m1
+// cg_a) with G(s) = sum_i w_i e^{2 pi i r_i s}.  G is tabulated at s_k =
+// (k - K0) delta (one thread per k, the radii summed in order) and read back
+// by 8-point Lagrange interpolation: G has at most half a turn per unit of s
+// (|r| <= 1/2), so delta = 1/32 leaves ~1e-11 relative error.
+__global__ void k_toep_gtable(const double *__restrict__ r, const double *__restrict__ w, int np,
+                              double delta, int K0, int Ns, double2 *__restrict__ G)
 {
-    const size_t N = (size_t)N0 * N1;
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 4 * N) return;
-    const int q = (int)(i / N), r = (int)(i - (size_t)q * N);
-    const int a = r / N1, cc = r - a * N1;
-    const int m0 = a - N0 / 2 + ((q >> 1) ? N0 / 2 : -N0 / 2);
-    const int m1 = cc - N1 / 2 + ((q & 1) ? N1 / 2 : -N1 / 2);
-    if (m0 <= -N0 || m0 >= N0 || m1 <= -N1 || m1 >= N1) return;
-    circ[(size_t)(m0 < 0 ? m0 + n0 : m0) * n1 + (m1 < 0 ? m1 + n1 : m1)] = Kq[i];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= Ns) return;
+    const double sv = (k - K0) * delta;
+    double re = 0, im = 0;
+    for (int i = 0; i < np; i++) {
+        double sn, cs;
+        sincospi(2.0 * r[i] * sv, &sn, &cs);
+        const double wi = w ? w[i] : 1.0;
+        re = fma(wi, cs, re);
+        im = fma(wi, sn, im);
+    }
+    G[k] = make_double2(re, im);
 }
 
-// The circulant's DFT (row-major n0 x n1) divided by n0 n1, in the order
-// k_col_toeplitz<R1, R2> reads it: [block of 4 columns][k2][k1][column],
+// circ[l0][l1] = K[m] for the signed indices m = (l0, l1) (mod nt) with
+// |m0| < N0, |m1| < N1, else 0; the lines summed in order.
+__global__ void k_toep_circ(const double2 *__restrict__ G, double delta, int K0,
+                            const double *__restrict__ sg, const double *__restrict__ cg, int A,
+                            int N0, int N1, int nt, double2 *__restrict__ circ)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)nt * nt) return;
+    const int l0 = (int)(i / nt), l1 = (int)(i - (size_t)l0 * nt);
+    const int m0 = l0 < nt / 2 ? l0 : l0 - nt, m1 = l1 < nt / 2 ? l1 : l1 - nt;
+    double re = 0, im = 0;
+    if (m0 > -N0 && m0 < N0 && m1 > -N1 && m1 < N1) {
+        // reciprocals of the Lagrange weights' denominators for the nodes
+        // -3..4: 1 / prod_{l != j} (j - l)
+        constexpr double rden[8] = {-1.0 / 5040, 1.0 / 720, -1.0 / 240, 1.0 / 144,
+                                    -1.0 / 144,  1.0 / 240, -1.0 / 720, 1.0 / 5040};
+        const double inv = 1.0 / delta;
+        for (int a = 0; a < A; a++) {
+            const double u = fma((double)m0, sg[a], (double)m1 * cg[a]) * inv + K0;
+            const double fu = floor(u);
+            const double t = u - fu;  // in [0, 1): nodes at t - (j - 3)
+            const int k0 = (int)fu - 3;
+            double d[8], pre[8], suf[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) d[j] = t - (j - 3);
+            pre[0] = 1.0;
+#pragma unroll
+            for (int j = 1; j < 8; j++) pre[j] = pre[j - 1] * d[j - 1];
+            suf[7] = 1.0;
+#pragma unroll
+            for (int j = 6; j >= 0; j--) suf[j] = suf[j + 1] * d[j + 1];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const double wj = pre[j] * suf[j] * rden[j];
+                const double2 gv = G[k0 + j];
+                re = fma(wj, gv.x, re);
+                im = fma(wj, gv.y, im);
+            }
+        }
+    }
+    circ[i] = make_double2(re, im);
+}
+
+// The circulant's DFT (row-major nt x nt, FP64) divided by nt^2, in the
+// order k_col_toeplitz<R1, R2> reads it: [block of 4 columns][k2][k1][column],
 // frequency row l0 = k1 + R1 k2.
 template <typename T>
-__global__ void k_toep_layout(const cplx_t<T> *__restrict__ F, int n0, int n1, int R1, int R2,
+__global__ void k_toep_layout(const double2 *__restrict__ F, int n0, int n1, int R1, int R2,
                               cplx_t<T> *__restrict__ khat)
 {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (size_t)n0 * n1) return;
     const int l0 = (int)(i / n1), l1 = (int)(i - (size_t)l0 * n1);
     const int k1 = l0 % R1, k2 = l0 / R1, cb = l1 >> 2, c = l1 & 3;
-    const T s = T(1) / ((T)n0 * (T)n1);
-    const cplx_t<T> v = F[i];
-    khat[(((size_t)cb * R2 + k2) * R1 + k1) * 4 + c] = mkc<T>(v.x * s, v.y * s);
+    const double sc = 1.0 / ((double)n0 * (double)n1);
+    const double2 v = F[i];
+    khat[(((size_t)cb * R2 + k2) * R1 + k1) * 4 + c] = mkc<T>((T)(v.x * sc), (T)(v.y * sc));
 }
 
 // ================================================================ K4b column IFFT
@@ -2028,16 +2079,18 @@ template <typename T> int NfftDev<T>::autotune(const NfftTables &t, cudaStream_t
 }
 
 // ================================================================ Toeplitz operator
-// K[m] for m in [-N, N)^2 as four adjoint NFFTs of the modulated weights
-// w_j e^{2 pi i s.x_j} (quadrant shifts s = (+-N0/2, +-N1/2): the adjoint
-// gives sum_j w_j e^{2 pi i s.x_j} e^{2 pi i k.x_j} = K[k + s] for k in
-// [-N/2, N/2)), the circulant embedding, its n0 x n1 DFT (cuFFT, once per
-// plan) and the column pass's layout.  In the plan's precision.
-template <typename T> int NfftDev<T>::toeplitz_init(const double *x, const T *w, cudaStream_t st)
+// K on the circulant in FP64 (k_toep_gtable, k_toep_circ), its nt x nt DFT
+// (cuFFT, FP64, once per plan), divided by nt^2 and laid out in the column
+// pass's read order in the plan's precision.
+template <typename T> int NfftDev<T>::toeplitz_init(const PolarGeom &g, cudaStream_t st)
 {
     if (!toeplitz_fits()) {
         set_error("Toeplitz operator: needs the fused four-step path on a square grid of 256, 512 "
                   "or 1024 points");
+        return NUDIM_EINVAL;
+    }
+    if (g.A <= 0 || (size_t)g.A * N1 != (size_t)M || !g.r || !g.sg || !g.cg) {
+        set_error("Toeplitz operator: the nodes must be A lines of N1 radii");
         return NUDIM_EINVAL;
     }
     if (toeplitz) return NUDIM_OK;
@@ -2047,73 +2100,65 @@ template <typename T> int NfftDev<T>::toeplitz_init(const double *x, const T *w,
     const char *eg = getenv("NUDIM_TOEPLITZ_GRID");
     const bool small = !(eg && !strcmp(eg, "nfft"));
     const int nt = (small && 2 * N0 - 1 <= 768 && n0 > 768) ? 768 : n0;
-    const size_t N = (size_t)N0 * N1, nn = (size_t)nt * nt;
-    std::vector<C> hv(4 * (size_t)M);
-    for (int q = 0; q < 4; q++) {
-        const double s0 = (q >> 1) ? N0 / 2 : -N0 / 2, s1 = (q & 1) ? N1 / 2 : -N1 / 2;
-        for (int j = 0; j < M; j++) {
-            // the phase's fractional part first: |s.x| reaches N/2 turns
-            double ph = s0 * x[2 * (size_t)j] + s1 * x[2 * (size_t)j + 1];
-            ph -= std::floor(ph);
-            hv[(size_t)q * M + j] = mkc<T>((T)std::cos(two_pi * ph), (T)std::sin(two_pi * ph));
-        }
-    }
+    const size_t nn = (size_t)nt * nt;
+    // G's table: |s| <= |m0| + |m1| < N0 + N1
+    const double delta = 1.0 / 32;
+    const int K0 = (int)std::ceil((N0 + N1) / delta) + 8, Ns = 2 * K0 + 1;
     std::vector<T> hones(std::max(N0, N1), T(1));
     std::vector<C> htw(nt);
     for (int k = 0; k < nt; k++) {
         const double a = -two_pi * (double)k / nt;
         htw[k] = mkc<T>((T)std::cos(a), (T)std::sin(a));
     }
-    void *dv = nullptr, *dk = nullptr, *dc = nullptr, *d1 = nullptr, *kh = nullptr, *dtw = nullptr;
+    void *dr = nullptr, *dw = nullptr, *dsg = nullptr, *dcg = nullptr, *dG = nullptr, *dc = nullptr;
+    void *d1 = nullptr, *kh = nullptr, *dtw = nullptr;
     // temporaries released stream-ordered after their last use; on failure
     // the kept buffers too
     auto done = [&](int e) {
-        for (void *q : {dv, dk, dc})
+        for (void *q : {dr, dw, dsg, dcg, dG, dc})
             if (q) cudaFreeAsync(q, st);
         if (e) {
-            if (d1) cudaFreeAsync(d1, st);
-            if (kh) cudaFreeAsync(kh, st);
-            if (dtw) cudaFreeAsync(dtw, st);
+            for (void *q : {d1, kh, dtw})
+                if (q) cudaFreeAsync(q, st);
         }
         return e;
     };
-    int rc = upload_async(&dv, hv.data(), sizeof(C) * hv.size(), st);
+    int rc = upload_async(&dr, g.r, sizeof(double) * N1, st);
+    if (!rc && g.wr) rc = upload_async(&dw, g.wr, sizeof(double) * N1, st);
+    if (!rc) rc = upload_async(&dsg, g.sg, sizeof(double) * g.A, st);
+    if (!rc) rc = upload_async(&dcg, g.cg, sizeof(double) * g.A, st);
     if (!rc) rc = upload_async(&d1, hones.data(), sizeof(T) * hones.size(), st);
     if (!rc && nt != n0) rc = upload_async(&dtw, htw.data(), sizeof(C) * htw.size(), st);
     if (rc) return done(rc);
-    if (cudaMallocAsync(&dk, sizeof(C) * 4 * N, st) != cudaSuccess ||
-        cudaMallocAsync(&dc, sizeof(C) * nn, st) != cudaSuccess ||
+    if (cudaMallocAsync(&dG, sizeof(double2) * Ns, st) != cudaSuccess ||
+        cudaMallocAsync(&dc, sizeof(double2) * nn, st) != cudaSuccess ||
         cudaMallocAsync(&kh, sizeof(C) * nn, st) != cudaSuccess) {
         set_error("Toeplitz operator: out of device memory");
         return done(NUDIM_ECUDA);
     }
-    SpreadArgs<T> sa;
-    sa.f = (const C *)dv;
-    sa.f_stride = M;
-    sa.w = w;
-    CropArgs<T> ca;
-    ca.mode = CM_PLAIN;
-    ca.out = (C *)dk;
-    ca.out_stride = N;
-    if ((rc = adjoint(4, sa, ca, st))) return done(rc);
-    if (cudaMemsetAsync(dc, 0, sizeof(C) * nn, st) != cudaSuccess) {
-        set_error("Toeplitz operator: memset failed");
+    k_toep_gtable<<<(unsigned)ceil_div(Ns, 128), 128, 0, st>>>((const double *)dr,
+                                                               (const double *)dw, N1, delta, K0,
+                                                               Ns, (double2 *)dG);
+    ++g_launches;
+    k_toep_circ<<<(unsigned)ceil_div((long)nn, 128), 128, 0, st>>>(
+        (const double2 *)dG, delta, K0, (const double *)dsg, (const double *)dcg, g.A, N0, N1, nt,
+        (double2 *)dc);
+    ++g_launches;
+    if (cudaGetLastError() != cudaSuccess) {
+        set_error("Toeplitz operator: setup kernel launch failed");
         return done(NUDIM_ECUDA);
     }
-    k_toep_embed<T><<<(unsigned)ceil_div((long)(4 * N), 256), 256, 0, st>>>(
-        (const C *)dk, N0, N1, nt, nt, (C *)dc);
-    ++g_launches;
     cufftHandle h;
-    if ((rc = ctx_fft2d(ctx, nt, nt, 1, prec_of<T>(), &h))) return done(rc);
+    if ((rc = ctx_fft2d(ctx, nt, nt, 1, NUDIM_FP64, &h))) return done(rc);
     if (cufftSetStream(h, st) != CUFFT_SUCCESS) {
         set_error("Toeplitz operator: cufftSetStream failed");
         return done(NUDIM_ECUDA);
     }
-    if ((rc = fft_exec<T>(h, (C *)dc, CUFFT_FORWARD))) return done(rc);
+    if ((rc = fft_exec<double>(h, (double2 *)dc, CUFFT_FORWARD))) return done(rc);
     // the column pass's four-step split of the circulant's size
     const int R1 = nt == 256 ? 16 : nt == 768 ? 24 : 32, R2 = nt / R1;
-    k_toep_layout<T><<<(unsigned)ceil_div((long)nn, 256), 256, 0, st>>>((const C *)dc, nt, nt, R1,
-                                                                         R2, (C *)kh);
+    k_toep_layout<T><<<(unsigned)ceil_div((long)nn, 256), 256, 0, st>>>((const double2 *)dc, nt,
+                                                                         nt, R1, R2, (C *)kh);
     ++g_launches;
     if (cudaGetLastError() != cudaSuccess) {
         set_error("Toeplitz operator: setup kernel launch failed");
@@ -2217,8 +2262,8 @@ int NfftDev<T>::toeplitz_apply(int nplanes, const PadArgs<T> &pa, const CropArgs
     return NUDIM_OK;
 }
 
-template int NfftDev<double>::toeplitz_init(const double *, const double *, cudaStream_t);
-template int NfftDev<float>::toeplitz_init(const double *, const float *, cudaStream_t);
+template int NfftDev<double>::toeplitz_init(const PolarGeom &, cudaStream_t);
+template int NfftDev<float>::toeplitz_init(const PolarGeom &, cudaStream_t);
 template int NfftDev<double>::toeplitz_apply(int, const PadArgs<double> &,
                                              const CropArgs<double> &, cudaStream_t);
 template int NfftDev<float>::toeplitz_apply(int, const PadArgs<float> &, const CropArgs<float> &,

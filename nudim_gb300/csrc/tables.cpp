@@ -61,6 +61,25 @@ void equal_angle_sample_2d(double amin, double amax, double ainterval, int nx, d
     }
 }
 
+void polar_factors(double amin, double amax, double ainterval, int nx, double *r, double *sg,
+                   double *cg)
+{
+    // the same loops and operations as equal_angle_sample_2d: node (a, i) is
+    // (r[i] sg[a], r[i] cg[a]) up to the one rounding of the product
+    int ns = equal_angle_count(amin, amax, ainterval);
+    double angle = amin - ainterval;
+    for (int s = 0; s < ns; s++) {
+        angle += ainterval;
+        sg[s] = sin(angle / 180 * kRefPi);
+        cg[s] = cos(angle / 180 * kRefPi);
+    }
+    double step = 1.0 / nx, rr = -0.5 - step;
+    for (int i = 0; i < nx; i++) {
+        rr += step;
+        r[i] = rr;
+    }
+}
+
 void uniform_sample_2d(int nx, int nz, double *x)
 {
     double ix = 1.0 / nx, iz = 1.0 / nz, z0 = -0.5 - iz;

@@ -18,6 +18,10 @@ int grid_size(int N);  // n = 2 * next_pow2(N) (reconstruction.c:316, 390)
 // src/grid.c:84 / 78-97 / 100-133
 int equal_angle_count(double amin, double amax, double ainterval);
 void equal_angle_sample_2d(double amin, double amax, double ainterval, int nx, double *x);
+// The same node set in factored form: radii r[nx] (angle-independent) and the
+// lines' sin / cos (sg, cg: equal_angle_count(amin, amax, ainterval) each).
+void polar_factors(double amin, double amax, double ainterval, int nx, double *r, double *sg,
+                   double *cg);
 void uniform_sample_2d(int nx, int nz, double *x);
 // src/reconstruction.c:375-384
 int polar_lines(double gam_min, double interval, double padangle, double *pad_min,

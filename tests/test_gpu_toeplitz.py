@@ -6,13 +6,11 @@ same iterates in exact arithmetic.
 
   - FP64, weighted: the volume after the initial inverse and after 4 ER
     iterations within 1e-8 of the NFFT form (the two operators differ by the
-    NFFT's own approximation error; measured 5e-11 and 3e-11), R histories
-    at rtol 1e-8; unweighted: the initial volume within 1e-8 (measured
-    5e-11), the volume after 4 ER within 1e-6: without the density
-    weights the normal equations are ill-conditioned and the warm-started
-    solves amplify the operators' difference (measured 1.1e-8, about 100 x
-    the NFFT form's own change under a 1e-13 input perturbation, which
-    measures input rounding, not an operator change);
+    NFFT's own approximation error and the kernel's interpolation, ~1e-11;
+    measured 1.4e-11 and 2.5e-12), R histories at rtol 1e-8; unweighted
+    (ill-conditioned normal equations: the warm-started solves amplify any
+    operator difference): the initial volume within 1e-8 (measured 5.2e-11),
+    the volume after 4 ER within 1e-6 (measured 7.4e-11);
   - FP32: the Toeplitz form's distance from the FP64 NFFT form within 3 x the
     FP32 NFFT form's distance (and below 1e-4)."""
 import numpy as np
