@@ -10,7 +10,7 @@
  * uniform Z axis (equal to the NFFT's accuracy).  DFT: nudim_project_dft, the
  * reference's exact sums with its truncated PI.  An unknown method name, which
  * the reference leaves undefined (:229-242), is rejected.  Noise uses the
- * library's seeded Gaussian generator (--seed, added by this build; default
+ * library's seeded Gaussian generator (--seed, an addition; default
  * 0), not GSL's sampler.
  */
 #include <getopt.h>

@@ -10,7 +10,7 @@
  * iteration 0, "-parallel" file names, total-time line) and runs on one GPU:
  * MPI ranks do not exist here, so no rank-count check applies.
  *
- * Options added by this build (no collision with the reference's):
+ * Options added here (no collision with the reference's):
  *   --precision=FP64|MIXED   arithmetic form (default FP64)
  *   --correct=<k>            MIXED: FP64 corrective iteration every k (0: off)
  *   --device=<n>             CUDA device (default 0)
