@@ -1,9 +1,10 @@
 """The library's host tables (nudim_gb300/csrc/tables.cpp) on the CPU, through
 a g++-built ctypes shim: node sets against the golden vectors made by the
 reference's own grid.c, the polar-line range, line classification, Kaiser-
-Bessel window tables and the MT19937 stream against the oracle, and the CGNR
+Bessel window tables and the MT19937 stream against the oracle, the CGNR
 weights against reconstruction.c:415-426 restated here (same operation order,
-so bit for bit)."""
+so bit for bit), and the polar set's factored form (the Toeplitz operator's
+input) against the node set itself."""
 import ctypes as C
 import os
 import shutil
@@ -24,6 +25,8 @@ int lt_equal_angle_count(double a, double b, double d) { return equal_angle_coun
 void lt_equal_angle_sample_2d(double a, double b, double d, int nx, double *x)
 { equal_angle_sample_2d(a, b, d, nx, x); }
 void lt_uniform_sample_2d(int nx, int nz, double *x) { uniform_sample_2d(nx, nz, x); }
+void lt_polar_factors(double a, double b, double d, int nx, double *r, double *sg, double *cg)
+{ polar_factors(a, b, d, nx, r, sg, cg); }
 int lt_polar_lines(double gmin, double interval, double pad, double *lo, double *hi)
 { return polar_lines(gmin, interval, pad, lo, hi); }
 void lt_cgnr_weights(int A, int np, double pad, double *w) { cgnr_weights(A, np, pad, w); }
@@ -67,6 +70,7 @@ def lt(tmp_path_factory):
     L.lt_equal_angle_count.argtypes = [C.c_double] * 3
     L.lt_equal_angle_sample_2d.argtypes = [C.c_double] * 3 + [C.c_int, _dp]
     L.lt_uniform_sample_2d.argtypes = [C.c_int, C.c_int, _dp]
+    L.lt_polar_factors.argtypes = [C.c_double] * 3 + [C.c_int, _dp, _dp, _dp]
     L.lt_polar_lines.restype = C.c_int
     L.lt_polar_lines.argtypes = [C.c_double] * 3 + [C.POINTER(C.c_double)] * 2
     L.lt_cgnr_weights.argtypes = [C.c_int, C.c_int, C.c_double, _dp]
@@ -160,3 +164,19 @@ def test_mt19937_stream_matches_the_oracle(lt, orc):
     assert np.array_equal(a, orc.mt19937_uniform(5000, 0))
     lt.lt_mt19937(5489, 5000, a)
     assert np.array_equal(a, orc.mt19937_uniform(5000, 5489))
+
+
+@pytest.mark.parametrize("a,b,d,npx", [(-90, 90, 1, 384), (-88, 90, 2, 128), (-89.5, 90, 0.5, 96),
+                                       (-87, 90, 3, 320)])
+def test_polar_factors_reproduce_the_node_set(lt, a, b, d, npx):
+    """Node (line a, radius i) of equal_angle_sample_2d is exactly the
+    product r[i] * (sg[a], cg[a]) of the factors (the same loops and
+    operations, one rounding of the product)."""
+    ns = lt.lt_equal_angle_count(a, b, d)
+    x = np.zeros(ns * npx * 2)
+    lt.lt_equal_angle_sample_2d(a, b, d, npx, x)
+    r, sg, cg = np.zeros(npx), np.zeros(ns), np.zeros(ns)
+    lt.lt_polar_factors(a, b, d, npx, r, sg, cg)
+    x = x.reshape(ns, npx, 2)
+    assert np.array_equal(x[:, :, 0], np.outer(sg, r))
+    assert np.array_equal(x[:, :, 1], np.outer(cg, r))
