@@ -943,6 +943,7 @@ int nudim_job_set_projections(nudim_job *jb, const double *proj, size_t n)
         return NUDIM_EINVAL;
     }
     NfftDev<double> p1;
+    p1.trafo_only = true;  // one trafo of the tilt series: no adjoint lists
     int rc = p1.init(ctx, t1, st, &jb->ws);
     std::vector<void *> tmp;
     auto talloc = [&](size_t b) -> void * {

@@ -188,6 +188,8 @@ template <typename T> struct NfftDev {
     // caps on the trafo column width and the planes per spreading CTA for
     // init_fused (0: the defaults, or the NUDIM_TUNE_* environment knobs)
     int tune_bc = 0, tune_planes = 0;
+    // set before init: build only the trafo's lists (adjoint() then fails)
+    bool trafo_only = false;
     size_t smem_col = 0, smem_row = 0, smem_spread = 0, smem_colifft = 0;
     C *tw0 = nullptr, *tw1 = nullptr;
     int *blk_off = nullptr, *ent = nullptr, *band_off = nullptr, *band_node = nullptr;

@@ -1363,15 +1363,20 @@ __global__ void k_toep_gtable(const double *__restrict__ r, const double *__rest
 }
 
 // circ[l0][l1] = K[m] for the signed indices m = (l0, l1) (mod nt) with
-// |m0| < N0, |m1| < N1, else 0; the lines summed in order.
+// |m0| < N0, |m1| < N1, else 0; the lines summed in order.  The weights are
+// real, so K[-m] = conj(K[m]): a thread takes the m of rows l0 <= nt/2 (for
+// row 0 and row nt/2 the columns l1 <= nt/2) and also writes -m; every entry
+// is written once.
 __global__ void k_toep_circ(const double2 *__restrict__ G, double delta, int K0,
                             const double *__restrict__ sg, const double *__restrict__ cg, int A,
                             int N0, int N1, int nt, double2 *__restrict__ circ)
 {
+    const int h = nt / 2;
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (size_t)nt * nt) return;
+    if (i >= (size_t)(h + 1) * nt) return;
     const int l0 = (int)(i / nt), l1 = (int)(i - (size_t)l0 * nt);
-    const int m0 = l0 < nt / 2 ? l0 : l0 - nt, m1 = l1 < nt / 2 ? l1 : l1 - nt;
+    if ((l0 == 0 || l0 == h) && l1 > h) return;  // the mirror of a column l1 < h
+    const int m0 = l0 < h ? l0 : l0 - nt, m1 = l1 < h ? l1 : l1 - nt;
     double re = 0, im = 0;
     if (m0 > -N0 && m0 < N0 && m1 > -N1 && m1 < N1) {
         // reciprocals of the Lagrange weights' denominators for the nodes
@@ -1403,6 +1408,8 @@ __global__ void k_toep_circ(const double2 *__restrict__ G, double delta, int K0,
         }
     }
     circ[i] = make_double2(re, im);
+    const int r0 = l0 ? nt - l0 : 0, r1 = l1 ? nt - l1 : 0;  // -m (mod nt)
+    if (r0 != l0 || r1 != l1) circ[(size_t)r0 * nt + r1] = make_double2(re, -im);
 }
 
 // The circulant's DFT (row-major nt x nt, FP64) divided by nt^2, in the
@@ -1563,7 +1570,7 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     if (t.n1 < 4 || t.n0 < 8) return NUDIM_EINVAL;
     const int bca = 4;
     FusedLists<T> L;
-    if (build_fused_lists(t, bc, bca, sizeof(T) == 4, &L) != 0) {
+    if (build_fused_lists(t, bc, bca, sizeof(T) == 4, &L, !trafo_only) != 0) {
         set_error("fused NFFT list construction failed");
         return NUDIM_EINVAL;
     }
@@ -1579,7 +1586,7 @@ template <typename T> int NfftDev<T>::init_fused(const NfftTables &t, cudaStream
     // tiles of more than one range, with their partial slots, for the fix-up
     std::vector<int4> hu, hf;
     nextra = 0;
-    for (int i = 0; i < ntiles; i++) {
+    for (int i = 0; i < (trafo_only ? 0 : ntiles); i++) {
         const int t = L.band_ord[i], b0 = L.band_off[t], len = L.band_off[t + 1] - b0;
         const int nr = std::max(1, ceil_div(len, kGatherMaxEntries));
         for (int r = 0; r < nr; r++)
@@ -1904,6 +1911,10 @@ template <typename T>
 int NfftDev<T>::adjoint_fused(int nplanes, const SpreadArgs<T> &sa, const CropArgs<T> &ca,
                               cudaStream_t st)
 {
+    if (trafo_only) {
+        set_error("NFFT plan built for the trafo only has no adjoint");
+        return NUDIM_ESTATE;
+    }
     int chunk = fused_chunk(nplanes, (size_t)N0 * n1 + (size_t)n0 * n1 + 32 * (size_t)nextra);
     void *wsv;
     size_t nH = (size_t)N0 * n1 * chunk, nG = (size_t)n0 * n1 * chunk;
@@ -2140,7 +2151,7 @@ template <typename T> int NfftDev<T>::toeplitz_init(const PolarGeom &g, cudaStre
                                                                (const double *)dw, N1, delta, K0,
                                                                Ns, (double2 *)dG);
     ++g_launches;
-    k_toep_circ<<<(unsigned)ceil_div((long)nn, 128), 128, 0, st>>>(
+    k_toep_circ<<<(unsigned)ceil_div((long)(nt / 2 + 1) * nt, 128), 128, 0, st>>>(
         (const double2 *)dG, delta, K0, (const double *)dsg, (const double *)dcg, g.A, N0, N1, nt,
         (double2 *)dc);
     ++g_launches;

@@ -275,7 +275,8 @@ void fft_twiddles(int n, std::vector<double> *tw)
 }
 
 template <typename Wt>
-int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists<Wt> *L)
+int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists<Wt> *L,
+                      bool adjoint)
 {
     const int kWin = 2 * 6 + 2;
     if (BC <= 0 || t.n1 % BC) return -1;
@@ -395,6 +396,13 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
     // ---- adjoint lists: tiles of R x BCa grid points (one per warp lane);
     // per tile the nodes whose window meets it, ascending.  Tiles are
     // numbered block-major: tile = b * nbands + v.
+    if (!adjoint) {
+        L->band_off.assign(1, 0);
+        L->band_node.assign(1, 0);
+        L->band_w.alloc(0);
+        L->band_ord.clear();
+        return 0;
+    }
     const int nblka = L->nblka;
     // the blocks and bands met by node j's window (each once)
     auto visit = [&](int j, std::vector<int> &bstamp, std::vector<int> &vstamp, auto &&fn) {
@@ -473,7 +481,9 @@ int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, Fuse
     return 0;
 }
 
-template int build_fused_lists<float>(const NfftTables &, int, int, bool, FusedLists<float> *);
-template int build_fused_lists<double>(const NfftTables &, int, int, bool, FusedLists<double> *);
+template int build_fused_lists<float>(const NfftTables &, int, int, bool, FusedLists<float> *,
+                                      bool);
+template int build_fused_lists<double>(const NfftTables &, int, int, bool, FusedLists<double> *,
+                                       bool);
 
 }  // namespace nudim

@@ -73,9 +73,12 @@ template <typename W> struct FusedLists {
 
 // BC a power of two dividing n1; BCa a power of two <= 32 dividing n1.
 // Returns 0, -1 (bad shape) or -2 (a window meets one trafo block twice:
-// the grid is too narrow for column blocks of BC).
+// the grid is too narrow for column blocks of BC).  adjoint = false leaves
+// the adjoint lists without entries (band_off = band_node = {0}, no
+// weights): a plan that only runs the trafo.
 template <typename W>
-int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists<W> *L);
+int build_fused_lists(const NfftTables &t, int BC, int BCa, bool pair_rows, FusedLists<W> *L,
+                      bool adjoint = true);
 
 // Spreading tile lists of the grid path: node ids whose window touches each
 // ty x tx tile of the n0 x n1 grid, ascending, CSR layout.
