@@ -156,16 +156,35 @@ int build_nfft_tables(int N0, int N1, int M, const double *x, int ty, int tx, Nf
     t->u0.assign(M, 0);
     t->u1.assign(M, 0);
     t->psi.assign((size_t)M * 2 * kW, 0.0);
+    // A node whose coordinate equals that of an earlier node of the same
+    // part (the previous node, or the node `per` earlier: a uniform grid's
+    // rows repeat both) copies its window values instead of evaluating the
+    // Kaiser-Bessel function again; the values are the same either way.
+    int per = 0;
+    for (int j = 1; j < M && j < 65536; j++)
+        if (x[2 * (size_t)j] == x[0]) {
+            per = j;
+            break;
+        }
     parallel_for(M, 2048, [&](int j0, int j1, int) {
         for (int j = j0; j < j1; j++) {
             for (int d = 0; d < 2; d++) {
                 int n = d ? t->n1 : t->n0;
                 double b = d ? b1 : b0;
-                double xn = x[2 * (size_t)j + d] * (double)n;
+                const double xv = x[2 * (size_t)j + d];
+                double xn = xv * (double)n;
                 int u = (int)floor(xn) - kM;
                 (d ? t->u1 : t->u0)[j] = u;
                 double *ps = t->psi.data() + (size_t)j * 2 * kW + (size_t)d * kW;
-                for (int s = 0; s < kW; s++) ps[s] = kb_phi(xn - (double)(u + s), b);
+                int src = -1;
+                if (j > j0 && x[2 * (size_t)(j - 1) + d] == xv) src = j - 1;
+                else if (per && j - per >= j0 && x[2 * (size_t)(j - per) + d] == xv) src = j - per;
+                if (src >= 0) {
+                    const double *q = t->psi.data() + (size_t)src * 2 * kW + (size_t)d * kW;
+                    for (int s = 0; s < kW; s++) ps[s] = q[s];
+                } else {
+                    for (int s = 0; s < kW; s++) ps[s] = kb_phi(xn - (double)(u + s), b);
+                }
             }
         }
     });
