@@ -180,3 +180,21 @@ def test_polar_factors_reproduce_the_node_set(lt, a, b, d, npx):
     x = x.reshape(ns, npx, 2)
     assert np.array_equal(x[:, :, 0], np.outer(sg, r))
     assert np.array_equal(x[:, :, 1], np.outer(cg, r))
+
+
+@pytest.mark.parametrize("npx,nz,N0,N1", [(64, 48, 48, 32), (40, 20, 24, 20)])
+def test_window_tables_of_repeated_coordinates(lt, npx, nz, N0, N1):
+    """A uniform grid's nodes repeat their coordinates row by row; the
+    tables give every node the window values of that node alone (the same
+    as a table built for it by itself), bit for bit."""
+    M = npx * nz
+    x = np.zeros(M * 2)
+    lt.lt_uniform_sample_2d(npx, nz, x)
+    u0, u1, psi = np.zeros(M, np.int32), np.zeros(M, np.int32), np.zeros(M * 28)
+    assert lt.lt_window(N0, N1, M, x, u0, u1, psi) == 0
+    psi = psi.reshape(M, 28)
+    for j in list(range(0, M, 37)) + [M - 1]:
+        a0, a1, p1 = np.zeros(1, np.int32), np.zeros(1, np.int32), np.zeros(28)
+        assert lt.lt_window(N0, N1, 1, np.ascontiguousarray(x[2 * j:2 * j + 2]), a0, a1, p1) == 0
+        assert (a0[0], a1[0]) == (u0[j], u1[j])
+        assert np.array_equal(p1, psi[j])
